@@ -1,0 +1,194 @@
+/*
+ * pmgb.h - C ABI of the GB300-native PM / P3M force-and-step path.
+ *
+ * Plain C: handles, plain pointers and sizes, int status codes; no C++ or torch types.  Every
+ * entry point replaces one piece of the reference's PMMethod / PMMethodGPU / P3MMethod /
+ * ChainingMesh call surface (paths below are within the reference project); the C++ facade in
+ * include/pmgb/ and the Python mirror in particlesimulation_gb300/ sit on top of it.
+ *
+ * Units.  Inputs are in the caller's "original" units, as the reference's constructors take
+ * them.  Inside a handle everything is kept in the reference's code units (x/H, v*DT/H,
+ * a*DT^2/H, m*4*pi*G*DT^2/H^3; include/unitConversions.h:8-50).  Getters take a `units`
+ * argument.
+ *
+ * Threading.  Each handle owns one CUDA stream and all of its device memory.  Handles are
+ * independent; calls on one handle are not thread-safe.  No call throws; failures return a
+ * status and pmgb_last_error() describes the last one.
+ */
+#ifndef PMGB_H
+#define PMGB_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define PMGB_OK 0
+#define PMGB_EINVAL 1   /* bad argument (reference: std::invalid_argument) */
+#define PMGB_ECUDA 2    /* a CUDA call failed */
+#define PMGB_EESCAPED 3 /* a particle left the computational box; the run stopped there */
+#define PMGB_ETIMEOUT 4 /* a bounded device wait gave up */
+#define PMGB_ENOMEM 5   /* device allocation failed */
+
+/* ---- enums: same names order and values as the reference ---- */
+/* InterpolationScheme (include/pmConfig.h:3) */
+#define PMGB_NGP 0
+#define PMGB_CIC 1
+#define PMGB_TSC 2
+/* FiniteDiffScheme (include/pmConfig.h:4) */
+#define PMGB_TWO_POINT 0
+#define PMGB_FOUR_POINT 1
+/* GreensFunction (include/pmConfig.h:5) */
+#define PMGB_DISCRETE_LAPLACIAN 0
+#define PMGB_S1_OPTIMAL 1
+#define PMGB_S2_OPTIMAL 2
+#define PMGB_POOR_MAN 3
+/* CloudShape (include/greensFunctions.h:7) */
+#define PMGB_S1 0
+#define PMGB_S2 1
+/* units of getters */
+#define PMGB_UNITS_CODE 0
+#define PMGB_UNITS_ORIGINAL 1
+/* external field kinds: the reference passes a std::function (include/pmMethod.h:17); on the
+ * device it is an enum with parameters.  SPH_RAD_DECR = sphRadDecrField(pos, center, R, M, G)
+ * (source/externalFields.cpp:4-15). */
+#define PMGB_EXT_NONE 0
+#define PMGB_EXT_SPH_RAD_DECR 1
+
+typedef struct pmgb_external_field {
+  int kind;
+  float center[3];
+  float R, M, G;
+} pmgb_external_field;
+
+/* Arguments of PMMethod(state, masses, effectiveBoxSize, externalField, externalPotential,
+ * H, DT, G, is, fds, gFunc, particleDiameter, grid) (include/pmMethod.h:14-26) with the grid
+ * given by its point counts, as PMMethodGPU takes it (include_gpu/PMMethodGPU.h:14-27). */
+typedef struct pmgb_pm_config {
+  int grid[3];          /* gridPoints (x, y, z); powers of two, 8..512 */
+  float box[3];         /* effectiveBoxSize, original units */
+  float H, DT, G;
+  int interpolation;    /* PMGB_NGP / PMGB_CIC / PMGB_TSC */
+  int finite_diff;      /* PMGB_TWO_POINT / PMGB_FOUR_POINT */
+  int greens;           /* PMGB_DISCRETE_LAPLACIAN / ... */
+  float particle_diameter; /* original units */
+  pmgb_external_field ext;
+  /* PM-only runs re-sort particles every `sort_interval` steps (results do not depend on the
+   * order; only locality does).  0 = default (8). */
+  int sort_interval;
+  /* 0: the reference's isolated setup (particles must stay in [0, box]; leaving it stops a
+   * run, PMGB_EESCAPED).  1: periodic box equal to the mesh: positions wrap after each drift and
+   * there is no escape test (the reference has no periodic mode; mesh indices always wrap). */
+  int periodic;
+} pmgb_pm_config;
+
+/* Arguments of P3MMethod(pm, compBoxSize, cutoffRadius, particleDiameter, H, softeningLength,
+ * cloudShape, useSRForceTable, enableYSorting) (include/p3mMethod.h:13-26). */
+typedef struct pmgb_p3m_config {
+  float comp_box[3];   /* compBoxSize, original units */
+  float cutoff;        /* cutoffRadius, original units */
+  float particle_diameter;
+  float softening;     /* softeningLength */
+  int cloud_shape;     /* PMGB_S1 / PMGB_S2 */
+  int use_table;       /* useSRForceTable (1 = 500-entry table, 0 = direct formula) */
+  int y_sorting;       /* enableYSorting: cell lists ordered by y (ties by index) or by
+                          descending index, exactly as ChainingMesh::fillWithYSorting / fill */
+} pmgb_p3m_config;
+
+typedef struct pmgb_pm pmgb_pm;   /* PMMethod / PMMethodGPU */
+typedef struct pmgb_p3m pmgb_p3m; /* P3MMethod (borrows a pmgb_pm) */
+
+/* ---------------------------------------------------------------- PM ---------------- */
+
+/* PMMethodGPU::PMMethodGPU (source/PMMethodGPU.cu:32-68): copies state (n positions then n
+ * velocities, xyz triplets, original units) and masses to the device, converting to code units.
+ * Precomputes the influence function (initGreensFunction, source/pmMethod.cpp:164-185) in FP64
+ * on the device. */
+int pmgb_pm_create(const pmgb_pm_config* cfg, int n, const float* state, const float* masses,
+                   pmgb_pm** out);
+/* ~PMMethodGPU (source/PMMethodGPU.cu:70-73). */
+int pmgb_pm_destroy(pmgb_pm* pm);
+
+/* PMMethod::initGreensFunction (source/pmMethod.cpp:164-185); also done by create. */
+int pmgb_pm_init_greens_function(pmgb_pm* pm);
+
+/* PMMethod::pmMethodStep (source/pmMethod.cpp:137-144): accelerations at the current
+ * positions (deposit, FFT, influence function, inverse FFT, finite-difference field,
+ * interpolation, external field).  No kick, no drift. */
+int pmgb_pm_method_step(pmgb_pm* pm);
+
+/* PMMethod::run (source/pmMethod.cpp:62-135) without recorder or diagnostics: initial force,
+ * half kick, then sim_length + 1 drift / force / kick iterations, stopping on an escaped
+ * particle exactly where the reference breaks.  Returns PMGB_EESCAPED in that case and
+ * *steps_done = completed iterations. */
+int pmgb_pm_run(pmgb_pm* pm, int sim_length, int* steps_done);
+
+/* The body of PMMethod::run's loop (source/pmMethod.cpp:79-122: drift, force, kick) repeated
+ * n_steps times, continuing from the state run() or a previous advance left (positions at an
+ * integer step, velocities half a step ahead).  Stops on an escaped particle like run().
+ * *device_ms (may be NULL) receives the device time of the whole call, measured with CUDA
+ * events on the handle's stream. */
+int pmgb_pm_advance(pmgb_pm* pm, int n_steps, int* steps_done, float* device_ms);
+
+/* PMMethod::getParticles (include/pmMethod.h:33): positions, velocities (half-step, as the
+ * reference stores them) and accelerations of the particles in their original index order.
+ * Any pointer may be NULL.  units = PMGB_UNITS_CODE or PMGB_UNITS_ORIGINAL (accelerations are
+ * converted with accelerationToOriginalUnits). */
+int pmgb_pm_get_particles(pmgb_pm* pm, float* pos, float* vel, float* acc, int units);
+
+/* PMMethodGPU::copyParticlesHostToDevice (include_gpu/PMMethodGPU.h:47): replace positions and
+ * velocities (original index order, `units`) of all particles. */
+int pmgb_pm_set_particles(pmgb_pm* pm, const float* pos, const float* vel, int units);
+
+/* PMMethod::escapedComputationalBox (source/pmMethod.cpp:146-156), on the device. */
+int pmgb_pm_escaped(pmgb_pm* pm, int* escaped);
+
+/* PMMethodGPU::copyGridDensityToHost / copyGridPotentialToHost + getGridDensity /
+ * getGridPotential (include_gpu/PMMethodGPU.h:48-55): the last step's density and potential
+ * meshes, nx*ny*nz floats, x fastest, code units. */
+int pmgb_pm_get_density(pmgb_pm* pm, float* density);
+int pmgb_pm_get_potential(pmgb_pm* pm, float* potential);
+/* The influence function as applied: (nx/2+1)*ny*nz floats (x fastest), already symmetrised
+ * over k and -k and divided by nx*ny*nz (the inverse FFT's 1/N, folded in). */
+int pmgb_pm_get_greens_function(pmgb_pm* pm, float* ghat);
+
+/* Device time of each stage of the last pmgb_pm_method_step / p3m force, in milliseconds:
+ * [sort, deposit, fft_forward+green+inverse, interpolation, pair pass]. */
+int pmgb_pm_stage_times(pmgb_pm* pm, float* ms5);
+
+/* Number of particles and the grid of a handle. */
+int pmgb_pm_size(pmgb_pm* pm, int* n, int* grid3);
+
+/* ---------------------------------------------------------------- P3M --------------- */
+
+/* P3MMethod::P3MMethod (source/p3mMethod.cpp:19-48): chaining mesh and short-range force
+ * table.  Borrows `pm` (which must outlive the P3M handle) and adds the short-range pair pass
+ * to every force evaluation of that PM handle while it exists. */
+int pmgb_p3m_create(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out);
+int pmgb_p3m_destroy(pmgb_p3m* p3m);
+
+/* One P3M force evaluation: pmMethodStep + calculateShortRangeForces + correctAccelerations
+ * (source/p3mMethod.cpp:63-73, 168-192, 50-57).  No kick, no drift. */
+int pmgb_p3m_force(pmgb_p3m* p3m);
+
+/* P3MMethod::run (source/p3mMethod.cpp:59-166) without recorder or diagnostics. */
+int pmgb_p3m_run(pmgb_p3m* p3m, int sim_length, int* steps_done);
+
+/* ChainingMesh cell lists of the last force evaluation (source/chainingMesh.cpp:20-58):
+ * order[] = particle ids cell after cell (cell index x + y*Mx + z*Mx*My), counts[] = list
+ * length per cell (Mx*My*Mz ints).  dims may be queried alone (order = counts = NULL). */
+int pmgb_p3m_get_cell_lists(pmgb_p3m* p3m, int* order, int* counts, int* dims3);
+
+/* The 500-entry short-range force table (initSRForceTable, source/p3mMethod.cpp:275-294) and
+ * its r^2 spacing, code units. */
+int pmgb_p3m_get_sr_table(pmgb_p3m* p3m, float* table500, float* delta_sq);
+
+/* ---------------------------------------------------------------- misc -------------- */
+const char* pmgb_last_error(void);
+/* Library build identification (architecture string). */
+const char* pmgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PMGB_H */

@@ -1,0 +1,234 @@
+// pair.cu - the P3M short-range pair pass on the chaining mesh.
+//
+// Restates P3MMethod::calculateShortRangeForces / updateSRForces / correctAccelerations
+// (reference source/p3mMethod.cpp:50-57, 168-192, 247-273, 296-322): every particle pair closer
+// than the cutoff in the same or adjacent chaining cells (non-periodic) adds
+//   F_ij = m_i m_j (T[t] + (xi - t) (T[t+1] - T[t])) r_ij,   xi = |r_ij|^2 / delta^2, t = int(xi)
+// from the 500-entry table (initSRForceTable, 275-294), or the direct S1/S2 formula
+// (shortRangeForce, 220-238) when the table is off; the acceleration gains F_i / m_i.
+//
+// GPU formulation.  The reference walks 13 half-shell neighbour cells and scatters -F_ij into
+// per-neighbour slots of j.  Here each particle gathers from all 27 cells (each pair is
+// evaluated twice, once per side), so no scatter, no atomics and a deterministic result.
+// Work items are 32-particle slices of one cell (the cells are y-sorted, so a slice spans a
+// narrow y range); a warp takes items from a global counter (dense cells cost more, the counter
+// balances).  For each neighbour cell a lane binary-searches the y window
+// [y_min - re, y_max + re] of the slice in that cell's y-sorted list (pairs outside it fail the
+// cutoff test anyway, as the reference's early break assumes); candidate j particles are loaded
+// 32 at a time, one per lane, and broadcast with shuffles.  Sums are FP32 per 32-particle chunk,
+// chunks are added with Kahan compensation.
+//
+// The epilogue adds the PM acceleration and, in a run, applies the kick, the drift, the unit
+// round trip and the escape test, writing the new state to separate buffers (other warps still
+// read the old positions).
+#include "common.cuh"
+
+namespace pmgb {
+
+struct ChainDimsP {
+  int Mx, My, Mz;
+  int ncells;
+};
+
+constexpr int PAIR_THREADS = 256;
+constexpr int PAIR_WARPS = PAIR_THREADS / 32;
+
+// referenceForceS1 / S2 (p3mMethod.cpp:194-218) and the direct short-range force magnitude
+// per unit r (shortRangeForce, 220-238): F = mi mj (-G/(r^2+eps^2) + R(r)) / r.
+__device__ float ref_force(int shape, float r, float a) {
+  const float G = 1.0f / (4.0f * 3.14159265f);
+  if (shape == 0) {
+    if (r >= a) return G / (r * r);
+    const float q = r / a;
+    return G / (a * a) * (8.0f * q - 9.0f * q * q + 2.0f * q * q * q * q);
+  }
+  const float u = 2.0f * r / a;
+  const float u2 = u * u, u3 = u2 * u, u4 = u2 * u2, u5 = u4 * u, u6 = u3 * u3;
+  if (u <= 1.0f)
+    return G / (35.0f * a * a) * (224.0f * u - 224.0f * u3 + 70.0f * u4 + 48.0f * u5 - 21.0f * u6);
+  if (u <= 2.0f)
+    return G / (35.0f * a * a) *
+           (12.0f / u2 - 224.0f + 896.0f * u - 840.0f * u2 + 224.0f * u3 + 70.0f * u4 - 48.0f * u5 + 7.0f * u6);
+  return G / (r * r);
+}
+
+__device__ __forceinline__ float direct_f(const PairParams& pp, float r2) {
+  const float G = 1.0f / (4.0f * 3.14159265f);
+  const float r = sqrtf(r2);
+  return (-G / (r2 + pp.eps2) + ref_force(pp.shape, r, pp.a)) / r;
+}
+
+// first index in [lo, hi) whose y >= v (lower) / > v (upper)
+__device__ __forceinline__ int y_lower(const float4* __restrict__ pm, int lo, int hi, float v) {
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(&pm[mid].y) < v) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+__device__ __forceinline__ int y_upper(const float4* __restrict__ pm, int lo, int hi, float v) {
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(&pm[mid].y) <= v) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
+  const float y = v - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
+
+__global__ void __launch_bounds__(PAIR_THREADS) pair_kernel(
+    const float4* __restrict__ pm, const float4* __restrict__ vi, const float4* __restrict__ acc_pm,
+    const int* __restrict__ cell_start, const int2* __restrict__ items, const u32* __restrict__ nitems_p,
+    u32* __restrict__ counter, ChainDimsP cd, PairParams pp, const float* __restrict__ table,
+    StepParams sp, float kick, int drift, int kdk, float4* __restrict__ pm_out,
+    float4* __restrict__ vi_out, float4* __restrict__ acc_out, unsigned long long* __restrict__ npairs,
+    int* stop) {
+  if (*stop) return;
+  __shared__ float2 tab[500];
+  for (int t = threadIdx.x; t < 499; t += PAIR_THREADS) {
+    const float a = table[t], b = table[t + 1];
+    tab[t] = make_float2(a, b - a);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const u32 nitems = *nitems_p;
+  unsigned long long my_pairs = 0;
+  for (;;) {
+    u32 it = 0;
+    if (lane == 0) it = atomicAdd(counter, 1u);
+    it = __shfl_sync(0xFFFFFFFFu, it, 0);
+    if (it >= nitems) break;
+    const int2 item = items[it];
+    const int cell = item.x;
+    const int cend = cell_start[cell + 1];
+    const int i = item.y + lane;
+    const bool valid = i < cend;
+    const int last = min(item.y + 31, cend - 1);
+    const float4 pi = pm[valid ? i : last];
+    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+
+    if (cell < cd.ncells) {
+      const int gx = cell % cd.Mx, gy = (cell / cd.Mx) % cd.My, gz = cell / (cd.Mx * cd.My);
+      // y range of the slice: lane 0 holds its first particle, lane 31 its last (lanes past
+      // the end of the cell load the last particle)
+      const float ylo = __shfl_sync(0xFFFFFFFFu, pi.y, 0) - pp.re;
+      const float yhi = __shfl_sync(0xFFFFFFFFu, pi.y, 31) + pp.re;
+      // lane k < 27 resolves neighbour k = (dx, dy, dz) in {-1,0,1}^3
+      int jb = 0, je = 0;
+      if (lane < 27) {
+        const int nx = gx + lane % 3 - 1, ny = gy + (lane / 3) % 3 - 1, nz = gz + lane / 9 - 1;
+        if (nx >= 0 && ny >= 0 && nz >= 0 && nx < cd.Mx && ny < cd.My && nz < cd.Mz) {
+          const int cn = nx + ny * cd.Mx + nz * cd.Mx * cd.My;
+          jb = cell_start[cn];
+          je = cell_start[cn + 1];
+          if (pp.ysort && je > jb) {
+            jb = y_lower(pm, jb, je, ylo);
+            je = y_upper(pm, jb, je, yhi);
+          }
+        }
+      }
+      for (int k = 0; k < 27; ++k) {
+        const int b = __shfl_sync(0xFFFFFFFFu, jb, k);
+        const int e = __shfl_sync(0xFFFFFFFFu, je, k);
+        for (int j0 = b; j0 < e; j0 += 32) {
+          const int jj = j0 + lane;
+          const float4 pj = jj < e ? pm[jj] : make_float4(3.0e30f, 3.0e30f, 3.0e30f, 0.f);
+          const int cnt = min(32, e - j0);
+          float px = 0.f, py = 0.f, pz = 0.f;
+          for (int s = 0; s < cnt; ++s) {
+            const float qx = __shfl_sync(0xFFFFFFFFu, pj.x, s);
+            const float qy = __shfl_sync(0xFFFFFFFFu, pj.y, s);
+            const float qz = __shfl_sync(0xFFFFFFFFu, pj.z, s);
+            const float qm = __shfl_sync(0xFFFFFFFFu, pj.w, s);
+            const float dx = pi.x - qx, dy = pi.y - qy, dz = pi.z - qz;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            if (valid && r2 < pp.re2) {
+              float f;
+              if (pp.use_table) {
+                const float xi = r2 * pp.inv_d2;
+                int t = (int)xi;
+                t = min(t, 498);
+                const float2 tv = tab[t];
+                f = qm * (tv.x + (xi - (float)t) * tv.y);
+              } else {
+                f = r2 > 0.f ? qm * direct_f(pp, r2) : 0.f;
+              }
+              px += f * dx;
+              py += f * dy;
+              pz += f * dz;
+              ++my_pairs;
+            }
+          }
+          kahan_add(sx, cx, px);
+          kahan_add(sy, cy, py);
+          kahan_add(sz, cz, pz);
+        }
+      }
+    }
+    if (valid) {
+      const float4 ap = acc_pm[i];
+      const float3 a = make_float3(ap.x + sx, ap.y + sy, ap.z + sz);
+      if (kdk) {
+        float4 p = pi, v = vi[i];
+        kick_drift(sp, p, v, a, kick, drift, stop);
+        pm_out[i] = p;
+        vi_out[i] = v;
+      }
+      acc_out[i] = make_float4(a.x, a.y, a.z, 0.f);
+    }
+  }
+  if (npairs) {
+    for (int o = 16; o > 0; o >>= 1) my_pairs += __shfl_xor_sync(0xFFFFFFFFu, my_pairs, o);
+    if (lane == 0 && my_pairs) atomicAdd(npairs, my_pairs);
+  }
+}
+
+// ------------------------------------------------------------------ work items ---------
+__global__ void item_count_kernel(const int* __restrict__ cell_start, int ncells_total,
+                                  u32* __restrict__ cnt, const int* stop) {
+  if (*stop) return;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells_total) return;
+  const int n = cell_start[c + 1] - cell_start[c];
+  cnt[c] = (u32)((n + 31) / 32);
+}
+
+__global__ void item_build_kernel(const int* __restrict__ cell_start, const u32* __restrict__ off,
+                                  int ncells_total, int2* __restrict__ items, const int* stop) {
+  if (*stop) return;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells_total) return;
+  const int b = cell_start[c], e = cell_start[c + 1];
+  u32 o = off[c];
+  for (int s = b; s < e; s += 32) items[o++] = make_int2(c, s);
+}
+
+int exclusive_scan(const u32* in, u32* out, int n, u32* total, cudaStream_t st);
+
+int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const int* cell_start,
+                int Mx, int My, int Mz, u32* item_cnt, u32* item_off, u32* nitems, int2* items,
+                u32* counter, const PairParams& pp, const float* table, const StepParams& sp,
+                float kick, int drift, int kdk, float4* pm_out, float4* vi_out, float4* acc_out,
+                unsigned long long* npairs, int* stop, int num_sms, cudaStream_t st) {
+  const int ncells = Mx * My * Mz;
+  const int ntot = ncells + 1;  // + the bucket of particles outside the chaining mesh
+  item_count_kernel<<<(ntot + 255) / 256, 256, 0, st>>>(cell_start, ntot, item_cnt, stop);
+  int rc = exclusive_scan(item_cnt, item_off, ntot, nitems, st);
+  if (rc) return rc;
+  item_build_kernel<<<(ntot + 255) / 256, 256, 0, st>>>(cell_start, item_off, ntot, items, stop);
+  PMGB_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(u32), st));
+  ChainDimsP cd{Mx, My, Mz, ncells};
+  pair_kernel<<<num_sms * 8, PAIR_THREADS, 0, st>>>(pm, vi, acc_pm, cell_start, items, nitems,
+                                                    counter, cd, pp, table, sp, kick, drift, kdk,
+                                                    pm_out, vi_out, acc_out, npairs, stop);
+  PMGB_LAUNCH_CHECK();
+  return PMGB_OK;
+}
+
+}  // namespace pmgb

@@ -1,0 +1,303 @@
+// sort.cu - particle ordering for the PM / P3M path.
+//
+// Two orders are produced on the device:
+//   * P3M: the reference's chaining-mesh cell lists (source/chainingMesh.cpp:20-58).  Cell =
+//     int(x/HC) per axis, flat x + y*Mx + z*Mx*My; within a cell ascending y with ties by
+//     ascending particle index (fillWithYSorting), or descending index (fill).  Particles are
+//     sorted by a 64-bit key (cell << 32 | order key) with a stable LSD radix sort, and runs of
+//     equal keys are put in index order afterwards, so the result is bit-identical to the
+//     reference's lists.
+//   * PM: Morton order of 4x4x4-cell bricks, for deposit / interpolation locality only (the
+//     density is computed in integer arithmetic, so results do not depend on the order).
+//
+// The radix sort is our own: per pass a block histogram, one exclusive scan, and a stable
+// scatter that ranks keys inside a warp with __match_any_sync.
+#include "common.cuh"
+
+namespace pmgb {
+
+constexpr int RS_THREADS = 256;
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_STRIPS = 16;                          // 32-key strips per warp
+constexpr int RS_TILE = RS_WARPS * RS_STRIPS * 32;     // 4096 keys per block
+
+__device__ __forceinline__ u32 lanemask_lt() {
+  u32 m;
+  asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__global__ void __launch_bounds__(RS_THREADS) rs_hist_kernel(const u64* __restrict__ keys, int n,
+                                                             int shift, u32 mask,
+                                                             u32* __restrict__ hist, int nblocks) {
+  __shared__ u32 h[256];
+  for (int d = threadIdx.x; d < 256; d += RS_THREADS) h[d] = 0;
+  __syncthreads();
+  const int base = blockIdx.x * RS_TILE;
+  const int lane = threadIdx.x & 31;
+  for (int off = 0; off < RS_TILE; off += RS_THREADS) {
+    int i = base + off + threadIdx.x;
+    bool valid = i < n;
+    u32 d = valid ? (u32)((keys[i] >> shift) & mask) : 0xFFFFFFFFu;
+    u32 peers = __match_any_sync(0xFFFFFFFFu, d);
+    if (valid && (__ffs(peers) - 1) == lane) atomicAdd(&h[d], (u32)__popc(peers));
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d <= (int)mask; d += RS_THREADS) hist[d * nblocks + blockIdx.x] = h[d];
+}
+
+// Single-CTA exclusive scan (in place allowed).  Used for the radix histograms (256 x blocks)
+// and for small count arrays.
+__global__ void __launch_bounds__(1024) exclusive_scan_kernel(const u32* __restrict__ in,
+                                                              u32* __restrict__ out, int n,
+                                                              u32* __restrict__ total) {
+  __shared__ u32 s[1024];
+  const int t = threadIdx.x;
+  const int chunk = (n + 1023) / 1024;
+  const int b = t * chunk, e = min(n, b + chunk);
+  u32 sum = 0;
+  for (int i = b; i < e; ++i) sum += in[i];
+  s[t] = sum;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    u32 v = t >= off ? s[t - off] : 0;
+    __syncthreads();
+    s[t] += v;
+    __syncthreads();
+  }
+  u32 run = s[t] - sum;
+  for (int i = b; i < e; ++i) {
+    u32 v = in[i];
+    out[i] = run;
+    run += v;
+  }
+  if (total && t == 1023) *total = s[1023];
+}
+
+__global__ void __launch_bounds__(RS_THREADS) rs_scatter_kernel(
+    const u64* __restrict__ kin, const u32* __restrict__ vin, u64* __restrict__ kout,
+    u32* __restrict__ vout, int n, int shift, u32 mask, const u32* __restrict__ hist,
+    int nblocks) {
+  __shared__ u32 wh[RS_WARPS][256];
+  __shared__ u32 gb[256];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = threadIdx.x; i < RS_WARPS * 256; i += RS_THREADS) (&wh[0][0])[i] = 0;
+  for (int d = threadIdx.x; d <= (int)mask; d += RS_THREADS) gb[d] = hist[d * nblocks + blockIdx.x];
+  __syncthreads();
+  u64 k[RS_STRIPS];
+  u32 v[RS_STRIPS], r[RS_STRIPS];
+  const int wbase = blockIdx.x * RS_TILE + warp * (RS_STRIPS * 32);
+  const u32 lt = lanemask_lt();
+#pragma unroll
+  for (int s = 0; s < RS_STRIPS; ++s) {
+    int i = wbase + s * 32 + lane;
+    bool valid = i < n;
+    k[s] = valid ? kin[i] : 0ull;
+    v[s] = valid ? vin[i] : 0u;
+    u32 d = valid ? (u32)((k[s] >> shift) & mask) : 0xFFFFFFFFu;
+    u32 peers = __match_any_sync(0xFFFFFFFFu, d);
+    u32 rank = __popc(peers & lt);
+    u32 pre = valid ? wh[warp][d] : 0u;
+    __syncwarp();
+    if (valid && rank == 0) wh[warp][d] = pre + __popc(peers);
+    __syncwarp();
+    r[s] = pre + rank;
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d <= (int)mask; d += RS_THREADS) {
+    u32 run = 0;
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; ++w) {
+      u32 t = wh[w][d];
+      wh[w][d] = run;
+      run += t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int s = 0; s < RS_STRIPS; ++s) {
+    int i = wbase + s * 32 + lane;
+    if (i < n) {
+      u32 d = (u32)((k[s] >> shift) & mask);
+      u32 dest = gb[d] + wh[warp][d] + r[s];
+      kout[dest] = k[s];
+      vout[dest] = v[s];
+    }
+  }
+}
+
+int radix_hist_blocks(int n) { return (n + RS_TILE - 1) / RS_TILE; }
+
+// Sorts (keys, vals) by key bits [0, nbits).  Ping-pongs with the alternates; on return
+// *keys / *vals point at the sorted data (the pointers may have been swapped).
+int radix_sort_pairs(u64** keys, u32** vals, u64** keys_alt, u32** vals_alt, u32* hist, int n,
+                     int nbits, cudaStream_t st) {
+  if (n <= 0) return PMGB_OK;
+  const int nb = radix_hist_blocks(n);
+  for (int shift = 0; shift < nbits; shift += 8) {
+    int bits = nbits - shift < 8 ? nbits - shift : 8;
+    u32 mask = (1u << bits) - 1u;
+    rs_hist_kernel<<<nb, RS_THREADS, 0, st>>>(*keys, n, shift, mask, hist, nb);
+    exclusive_scan_kernel<<<1, 1024, 0, st>>>(hist, hist, (int)(mask + 1) * nb, nullptr);
+    rs_scatter_kernel<<<nb, RS_THREADS, 0, st>>>(*keys, *vals, *keys_alt, *vals_alt, n, shift,
+                                                 mask, hist, nb);
+    PMGB_LAUNCH_CHECK();
+    u64* tk = *keys;
+    *keys = *keys_alt;
+    *keys_alt = tk;
+    u32* tv = *vals;
+    *vals = *vals_alt;
+    *vals_alt = tv;
+  }
+  return PMGB_OK;
+}
+
+int exclusive_scan(const u32* in, u32* out, int n, u32* total, cudaStream_t st) {
+  exclusive_scan_kernel<<<1, 1024, 0, st>>>(in, out, n, total);
+  PMGB_LAUNCH_CHECK();
+  return PMGB_OK;
+}
+
+// ------------------------------------------------------------------ keys --------------
+// Chaining-mesh cell of a code-unit position (ChainingMesh::tripleToFlatIndex); -1 outside.
+__device__ __forceinline__ int chain_cell(const ChainDims& c, float x, float y, float z) {
+  int cx = (int)__fdiv_rn(x, c.HCx), cy = (int)__fdiv_rn(y, c.HCy), cz = (int)__fdiv_rn(z, c.HCz);
+  if (cx < 0 || cy < 0 || cz < 0 || cx >= c.Mx || cy >= c.My || cz >= c.Mz) return -1;
+  return cx + cy * c.Mx + cz * c.Mx * c.My;
+}
+
+__global__ void chain_keys_kernel(const float4* __restrict__ pm, const float4* __restrict__ vi,
+                                  int n, ChainDims c, int ysort, int ncells,
+                                  const int* __restrict__ stop, u64* __restrict__ keys,
+                                  u32* __restrict__ vals) {
+  if (stop && *stop) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 p = pm[i];
+  int cell = chain_cell(c, p.x, p.y, p.z);
+  if (cell < 0) cell = ncells;  // outside the chaining mesh: last bucket, no pair forces
+  u32 lo;
+  if (ysort) {
+    lo = float_key(p.y);
+  } else {
+    int orig = __float_as_int(vi[i].w);
+    lo = 0xFFFFFFFFu - (u32)orig;  // ChainingMesh::fill inserts at the head: descending id
+  }
+  keys[i] = ((u64)(u32)cell << 32) | lo;
+  vals[i] = (u32)i;
+}
+
+// Runs of equal (cell, y) keys are ordered by original particle id, as the reference's
+// insertion keeps earlier particles first among equal y (chainingMesh.cpp:33-38).
+__global__ void fix_ties_kernel(const u64* __restrict__ keys, u32* __restrict__ vals,
+                                const float4* __restrict__ vi, int n, const int* __restrict__ stop) {
+  if (stop && *stop) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i + 1 >= n) return;
+  u64 k = keys[i];
+  if (keys[i + 1] != k) return;
+  if (i > 0 && keys[i - 1] == k) return;
+  int e = i + 1;
+  while (e + 1 < n && keys[e + 1] == k) ++e;
+  for (int a = i + 1; a <= e; ++a) {  // insertion sort of vals[i..e] by original id
+    u32 v = vals[a];
+    int ov = __float_as_int(vi[v].w);
+    int b = a - 1;
+    while (b >= i && __float_as_int(vi[vals[b]].w) > ov) {
+      vals[b + 1] = vals[b];
+      --b;
+    }
+    vals[b + 1] = v;
+  }
+}
+
+__device__ __forceinline__ u32 spread3(u32 x) {  // 10 bits -> every third bit
+  x &= 0x3FF;
+  x = (x | (x << 16)) & 0x030000FF;
+  x = (x | (x << 8)) & 0x0300F00F;
+  x = (x | (x << 4)) & 0x030C30C3;
+  x = (x | (x << 2)) & 0x09249249;
+  return x;
+}
+
+__global__ void brick_keys_kernel(const float4* __restrict__ pm, int n, MeshDims m, int bshift,
+                                  const int* __restrict__ stop, u64* __restrict__ keys,
+                                  u32* __restrict__ vals) {
+  if (stop && *stop) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 p = pm[i];
+  int ix = wrapi((int)floorf(p.x), m.nx) >> bshift;
+  int iy = wrapi((int)floorf(p.y), m.ny) >> bshift;
+  int iz = wrapi((int)floorf(p.z), m.nz) >> bshift;
+  keys[i] = (u64)(spread3(ix) | (spread3(iy) << 1) | (spread3(iz) << 2));
+  vals[i] = (u32)i;
+}
+
+// Permute particles into sorted order.  For the P3M order also records cell start offsets
+// (cell_start[c] = first sorted slot of cell c; cell_start[ncells + 1] = n).
+__global__ void gather_kernel(const u64* __restrict__ keys, const u32* __restrict__ vals, int n,
+                              const float4* __restrict__ pm_in, const float4* __restrict__ vi_in,
+                              float4* __restrict__ pm_out, float4* __restrict__ vi_out,
+                              int* __restrict__ cell_start, int ncells_total,
+                              const int* __restrict__ stop) {
+  if (stop && *stop) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  u32 s = vals[i];
+  pm_out[i] = pm_in[s];
+  vi_out[i] = vi_in[s];
+  if (cell_start) {
+    int c = (int)(keys[i] >> 32);
+    int prev = i == 0 ? -1 : (int)(keys[i - 1] >> 32);
+    for (int cc = prev + 1; cc <= c; ++cc) cell_start[cc] = i;
+    if (i == n - 1)
+      for (int cc = c + 1; cc <= ncells_total; ++cc) cell_start[cc] = n;
+  }
+}
+
+__global__ void fill_int_kernel(int* p, int n, int v) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
+// ------------------------------------------------------------------ host side ---------
+int launch_chain_keys(const float4* pm, const float4* vi, int n, ChainDims c, int ysort,
+                      const int* stop, u64* keys, u32* vals, cudaStream_t st) {
+  int ncells = c.Mx * c.My * c.Mz;
+  chain_keys_kernel<<<(n + 255) / 256, 256, 0, st>>>(pm, vi, n, c, ysort, ncells, stop, keys, vals);
+  PMGB_LAUNCH_CHECK();
+  return PMGB_OK;
+}
+
+int launch_fix_ties(const u64* keys, u32* vals, const float4* vi, int n, const int* stop,
+                    cudaStream_t st) {
+  fix_ties_kernel<<<(n + 255) / 256, 256, 0, st>>>(keys, vals, vi, n, stop);
+  PMGB_LAUNCH_CHECK();
+  return PMGB_OK;
+}
+
+int launch_brick_keys(const float4* pm, int n, MeshDims m, int bshift, const int* stop, u64* keys,
+                      u32* vals, cudaStream_t st) {
+  brick_keys_kernel<<<(n + 255) / 256, 256, 0, st>>>(pm, n, m, bshift, stop, keys, vals);
+  PMGB_LAUNCH_CHECK();
+  return PMGB_OK;
+}
+
+int launch_gather(const u64* keys, const u32* vals, int n, const float4* pm_in,
+                  const float4* vi_in, float4* pm_out, float4* vi_out, int* cell_start,
+                  int ncells_total, const int* stop, cudaStream_t st) {
+  if (n == 0) {
+    if (cell_start) {
+      fill_int_kernel<<<(ncells_total + 256) / 256, 256, 0, st>>>(cell_start, ncells_total + 1, 0);
+      PMGB_LAUNCH_CHECK();
+    }
+    return PMGB_OK;
+  }
+  gather_kernel<<<(n + 255) / 256, 256, 0, st>>>(keys, vals, n, pm_in, vi_in, pm_out, vi_out,
+                                                 cell_start, ncells_total, stop);
+  PMGB_LAUNCH_CHECK();
+  return PMGB_OK;
+}
+
+}  // namespace pmgb

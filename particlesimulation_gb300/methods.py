@@ -1,0 +1,254 @@
+"""Python mirror of the reference's PM / P3M call surface over the C ABI (include/pmgb.h).
+
+Names, argument order and meaning follow the reference (include/pmMethod.h:12-46,
+include_gpu/PMMethodGPU.h:12-55, include/p3mMethod.h:11-31, include/pmConfig.h:3-5,
+include/greensFunctions.h:7).  The differences are the ones a device path needs: the grid is
+given by its point counts (as PMMethodGPU takes it) and the external field is a description
+(``SphRadDecrField``) instead of a host callback.  Errors: invalid arguments raise ValueError
+(the reference throws std::invalid_argument), device failures raise PMGBError; an escaped
+particle stops ``run`` like the reference's loop break and is reported by its return value.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import UNITS_CODE, UNITS_ORIGINAL, check, lib
+
+
+class InterpolationScheme(enum.IntEnum):
+    NGP = 0
+    CIC = 1
+    TSC = 2
+
+
+class FiniteDiffScheme(enum.IntEnum):
+    TWO_POINT = 0
+    FOUR_POINT = 1
+
+
+class GreensFunction(enum.IntEnum):
+    DISCRETE_LAPLACIAN = 0
+    S1_OPTIMAL = 1
+    S2_OPTIMAL = 2
+    POOR_MAN = 3
+
+
+class CloudShape(enum.IntEnum):
+    S1 = 0
+    S2 = 1
+
+
+@dataclass(frozen=True)
+class SphRadDecrField:
+    """sphRadDecrField(pos, center, R, M, G) (reference source/externalFields.cpp:4-15)."""
+    center: tuple
+    R: float
+    M: float
+    G: float
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _f32(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+class PMMethod:
+    """PMMethodGPU(state, masses, effectiveBoxSize, externalField, externalPotential, H, DT, G,
+    is, fds, gFunc, particleDiameter, gridPoints) on the GB300 path.  ``state`` holds the N
+    positions followed by the N velocities (original units)."""
+
+    def __init__(self, state, masses, effectiveBoxSize, externalField, H, DT, G,
+                 interpolation: InterpolationScheme, finiteDiff: FiniteDiffScheme,
+                 greensFunction: GreensFunction, particleDiameter, gridPoints,
+                 sortInterval: int = 0, periodic: bool = False):
+        masses = _f32(masses).reshape(-1)
+        n = len(masses)
+        state = _f32(state, (2 * n, 3))
+        cfg = _lib.PMConfigC()
+        cfg.grid[:] = [int(g) for g in gridPoints]
+        cfg.box[:] = [float(b) for b in effectiveBoxSize]
+        cfg.H, cfg.DT, cfg.G = float(H), float(DT), float(G)
+        cfg.interpolation, cfg.finite_diff, cfg.greens = int(interpolation), int(finiteDiff), int(greensFunction)
+        cfg.particle_diameter = float(particleDiameter)
+        if externalField is not None:
+            cfg.ext.kind = 1
+            cfg.ext.center[:] = [float(c) for c in externalField.center]
+            cfg.ext.R, cfg.ext.M, cfg.ext.G = externalField.R, externalField.M, externalField.G
+        cfg.sort_interval = int(sortInterval)
+        cfg.periodic = int(bool(periodic))
+        self._cfg = cfg
+        self.N = n
+        self.H, self.DT, self.G = float(H), float(DT), float(G)
+        self.gridPoints = tuple(int(g) for g in gridPoints)
+        h = C.c_void_p()
+        check(lib().pmgb_pm_create(C.byref(cfg), n, _fp(state), _fp(masses), C.byref(h)))
+        self._h = h
+        self._p3m = None
+
+    # -- lifecycle --
+    def close(self):
+        if getattr(self, "_h", None):
+            if self._p3m is not None:
+                self._p3m.close()
+            check(lib().pmgb_pm_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- reference surface --
+    def getH(self):
+        return self.H
+
+    def getDT(self):
+        return self.DT
+
+    def getG(self):
+        return self.G
+
+    def initGreensFunction(self):
+        check(lib().pmgb_pm_init_greens_function(self._h))
+
+    def pmMethodStep(self):
+        check(lib().pmgb_pm_method_step(self._h))
+
+    def run(self, simLength: int):
+        """PMMethod::run without recorder: returns (escaped, steps_done)."""
+        done = C.c_int(0)
+        rc = check(lib().pmgb_pm_run(self._h, int(simLength), C.byref(done)))
+        return rc == _lib.PMGB_EESCAPED, done.value
+
+    def advance(self, nSteps: int):
+        """nSteps more iterations of run()'s loop body (drift, force, kick), continuing from the
+        state run() or a previous advance left.  Returns (escaped, steps_done, device_ms)."""
+        done = C.c_int(0)
+        ms = C.c_float(0)
+        rc = check(lib().pmgb_pm_advance(self._h, int(nSteps), C.byref(done), C.byref(ms)))
+        return rc == _lib.PMGB_EESCAPED, done.value, ms.value
+
+    def getParticles(self, units: str = "code"):
+        """(positions, velocities, accelerations), each (N, 3) float32 in original index order."""
+        n = self.N
+        pos = np.zeros((n, 3), np.float32)
+        vel = np.zeros((n, 3), np.float32)
+        acc = np.zeros((n, 3), np.float32)
+        u = UNITS_ORIGINAL if units == "original" else UNITS_CODE
+        check(lib().pmgb_pm_get_particles(self._h, _fp(pos), _fp(vel), _fp(acc), u))
+        return pos, vel, acc
+
+    def setParticles(self, pos, vel, units: str = "original"):
+        n = self.N
+        u = UNITS_ORIGINAL if units == "original" else UNITS_CODE
+        check(lib().pmgb_pm_set_particles(self._h, _fp(_f32(pos, (n, 3))), _fp(_f32(vel, (n, 3))), u))
+
+    def escapedComputationalBox(self) -> bool:
+        e = C.c_int(0)
+        check(lib().pmgb_pm_escaped(self._h, C.byref(e)))
+        return bool(e.value)
+
+    def getGridDensity(self):
+        nx, ny, nz = self.gridPoints
+        d = np.zeros(nx * ny * nz, np.float32)
+        check(lib().pmgb_pm_get_density(self._h, _fp(d)))
+        return d
+
+    def getGridPotential(self):
+        nx, ny, nz = self.gridPoints
+        d = np.zeros(nx * ny * nz, np.float32)
+        check(lib().pmgb_pm_get_potential(self._h, _fp(d)))
+        return d
+
+    def getGreensFunction(self):
+        """Influence function as applied: (nz, ny, nx//2+1), symmetrised, times 1/(nx ny nz)."""
+        nx, ny, nz = self.gridPoints
+        g = np.zeros(nz * ny * (nx // 2 + 1), np.float32)
+        check(lib().pmgb_pm_get_greens_function(self._h, _fp(g)))
+        return g.reshape(nz, ny, nx // 2 + 1)
+
+    def stageTimes(self):
+        t = np.zeros(5, np.float32)
+        check(lib().pmgb_pm_stage_times(self._h, _fp(t)))
+        return dict(zip(["sort", "deposit", "poisson", "interpolation", "pair"], t.tolist()))
+
+
+class P3MMethod:
+    """P3MMethod(pm, compBoxSize, cutoffRadius, particleDiameter, H, softeningLength,
+    cloudShape, useSRForceTable, enableYSorting) on the GB300 path; borrows ``pm``."""
+
+    def __init__(self, pm: PMMethod, compBoxSize, cutoffRadius, particleDiameter, H,
+                 softeningLength, cloudShape: CloudShape, useSRForceTable: bool = True,
+                 enableYSorting: bool = True):
+        if abs(float(H) - pm.H) > 0:
+            raise ValueError("P3MMethod H must equal the PM method's H")
+        cfg = _lib.P3MConfigC()
+        cfg.comp_box[:] = [float(b) for b in compBoxSize]
+        cfg.cutoff = float(cutoffRadius)
+        cfg.particle_diameter = float(particleDiameter)
+        cfg.softening = float(softeningLength)
+        cfg.cloud_shape = int(cloudShape)
+        cfg.use_table = int(bool(useSRForceTable))
+        cfg.y_sorting = int(bool(enableYSorting))
+        h = C.c_void_p()
+        check(lib().pmgb_p3m_create(pm._h, C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.pm = pm
+        pm._p3m = self
+
+    def close(self):
+        if getattr(self, "_h", None):
+            check(lib().pmgb_p3m_destroy(self._h))
+            self._h = None
+            self.pm._p3m = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def force(self):
+        """pmMethodStep + calculateShortRangeForces + correctAccelerations."""
+        check(lib().pmgb_p3m_force(self._h))
+
+    def run(self, simLength: int):
+        done = C.c_int(0)
+        rc = check(lib().pmgb_p3m_run(self._h, int(simLength), C.byref(done)))
+        return rc == _lib.PMGB_EESCAPED, done.value
+
+    def getCellLists(self):
+        """(order, counts, (Mx, My, Mz)) of the last force evaluation."""
+        dims = (C.c_int * 3)()
+        ip = C.POINTER(C.c_int)
+        check(lib().pmgb_p3m_get_cell_lists(self._h, ip(), ip(), dims))
+        mx, my, mz = dims[0], dims[1], dims[2]
+        counts = np.zeros(mx * my * mz, np.int32)
+        order = np.zeros(self.pm.N, np.int32)
+        check(lib().pmgb_p3m_get_cell_lists(self._h, order.ctypes.data_as(ip),
+                                            counts.ctypes.data_as(ip), dims))
+        return order[: counts.sum()], counts, (mx, my, mz)
+
+    def getSRForceTable(self):
+        t = np.zeros(500, np.float32)
+        d2 = C.c_float(0)
+        check(lib().pmgb_p3m_get_sr_table(self._h, _fp(t), C.byref(d2)))
+        return t, d2.value

@@ -1,0 +1,167 @@
+"""Generates tests/golden/*.npz from the reference's own CPU code (oracle/_ref/libpsref.so,
+compiled from the reference sources by oracle/Makefile).
+
+Run where the reference sources exist:  python tests/golden/make_golden.py
+Every case is a small seeded input; each fixture stores the inputs, the settings and the
+reference's outputs (float32), so tests on a machine without the reference still compare
+against the reference itself.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+
+
+def inputs(seed, n, lo, hi, clustered=True):
+    rng = np.random.default_rng(seed)
+    if clustered:
+        c = 0.5 * (lo + hi)
+        p = np.concatenate([rng.normal(c, 0.08 * (hi - lo), (n // 2, 3)),
+                            rng.uniform(lo, hi, (n - n // 2, 3))])
+        p = np.clip(p, lo, hi)
+    else:
+        p = rng.uniform(lo, hi, (n, 3))
+    v = rng.normal(0, 0.02, (n, 3))
+    m = rng.uniform(0.5, 1.5, n) / n
+    return p.astype(np.float32), v.astype(np.float32), m.astype(np.float32)
+
+
+def pm_cases():
+    H = 30.0 / 16
+    out = []
+    k = 0
+    for is_ in (0, 1, 2):
+        for fds in (0, 1):
+            for gf in (0, 1, 2, 3):
+                ext = (15.0, 15.0, 15.0, 3.0, 0.5, 1.0) if (k % 3 == 0) else ()
+                cfg = O.PMConfig(grid=(32, 32, 32), box=(30.0, 30.0, 30.0), H=H, DT=0.1, G=1.0,
+                                 interpolation=is_, finite_diff=fds, greens=gf, diameter=3 * H,
+                                 ext=ext)
+                out.append((f"pm_is{is_}_fd{fds}_gf{gf}", cfg))
+                k += 1
+    # non-cubic mesh, as the reference's galaxy demos use (128 x 128 x 64 scaled down)
+    cfg = O.PMConfig(grid=(32, 32, 16), box=(30.0, 30.0, 15.0), H=H, DT=0.1, G=1.0,
+                     interpolation=2, finite_diff=0, greens=0, diameter=0.0)
+    out.append(("pm_noncubic_tsc", cfg))
+    return out
+
+
+MESH_CASES = ("pm_is1_fd0_gf0", "pm_is2_fd0_gf2", "pm_is2_fd1_gf1", "pm_is0_fd0_gf3")
+
+
+def main():
+    assert O.build_ref(), "reference sources not found"
+    os.makedirs(HERE, exist_ok=True)
+    # ---- PM forces (single pmMethodStep after unit conversion and Green's function)
+    p, v, m = inputs(10, 600, 3.0, 27.0)
+    cases = {}
+    for name, cfg in pm_cases():
+        lo_hi = (3.0, 12.0) if cfg.grid[2] == 16 else (3.0, 27.0)
+        pp, vv, mm = (p, v, m) if cfg.grid[2] == 32 else inputs(11, 600, *lo_hi)
+        acc, dens, pot, grn = O.ref_pm_accel(cfg, pp, vv, mm, want_mesh=True)
+        d = dict(acc=acc, **_cfg_arrays(cfg))
+        if cfg.grid[2] != 32:
+            d.update(pos=pp, vel=vv, mass=mm)
+        if name in MESH_CASES:  # meshes for a few cases only (fixture size)
+            d.update(density=dens, potential=pot, green=grn)
+        cases[name] = d
+    cases["inputs"] = dict(pos=p, vel=v, mass=m)
+    np.savez_compressed(os.path.join(HERE, "pm_forces.npz"),
+                        **{f"{c}/{k}": a for c, d in cases.items() for k, a in d.items()})
+    # ---- P3M forces
+    H = 30.0 / 16
+    p, v, m = inputs(20, 3000, 4.0, 26.0)
+    cases = {}
+    for cs, gf in ((0, 1), (1, 2)):
+        for table in (1, 0):
+            for ys in (1, 0):
+                cfg = O.PMConfig(grid=(32, 32, 32), box=(30.0, 30.0, 30.0), H=H, DT=0.1, G=1.0,
+                                 interpolation=2, finite_diff=0, greens=gf, diameter=3 * H)
+                q = O.P3MConfig(comp_box=(30.0, 30.0, 30.0), cutoff=3 * H, diameter=3 * H,
+                                softening=0.0 if table else 0.2, cloud_shape=cs, use_table=table,
+                                y_sorting=ys)
+                acc = O.ref_p3m_accel(cfg, q, p, v, m)
+                cases[f"p3m_cs{cs}_t{table}_y{ys}"] = dict(acc=acc, **_cfg_arrays(cfg),
+                                                           **_p3m_arrays(q))
+    cases["inputs"] = dict(pos=p, vel=v, mass=m)
+    np.savez_compressed(os.path.join(HERE, "p3m_forces.npz"),
+                        **{f"{c}/{k}": a for c, d in cases.items() for k, a in d.items()})
+    # ---- chaining-mesh cell lists (code-unit positions), including exact y ties
+    rng = np.random.default_rng(30)
+    pc = rng.uniform(0, 16, (4000, 3)).astype(np.float32)
+    pc[:400, 1] = np.float32(7.25)                     # many equal y values
+    pc[400:440] = pc[440:480]                          # duplicated particles
+    q = O.P3MConfig(comp_box=(30.0, 30.0, 30.0), cutoff=3 * H, diameter=3 * H)
+    cl = {}
+    for ys in (1, 0):
+        order, counts, dims = O.ref_chaining_mesh(q, H, pc, ys)
+        cl[f"y{ys}/order"] = order
+        cl[f"y{ys}/counts"] = counts
+        cl[f"y{ys}/dims"] = np.array(dims, np.int32)
+    np.savez_compressed(os.path.join(HERE, "cell_lists.npz"), pos_code=pc, H=np.float32(H),
+                        **{f"q/{k}": a for k, a in _p3m_arrays(q).items()}, **cl)
+    # ---- short runs (run(simLength) from the reference, final state in original units)
+    p, v, m = inputs(40, 800, 8.0, 22.0)
+    runs = {}
+    cfg = O.PMConfig(grid=(32, 32, 32), box=(30.0, 30.0, 30.0), H=H, DT=0.1, G=1.0,
+                     interpolation=1, finite_diff=0, greens=0, diameter=0.0)
+    x, vv, esc = O.ref_run(cfg, None, p, v, m, 4)
+    runs["pm"] = dict(pos=p, vel=v, mass=m, pos_out=x, vel_out=vv, escaped=np.int32(esc),
+                      sim_length=np.int32(4), **_cfg_arrays(cfg))
+    cfg = O.PMConfig(grid=(32, 32, 32), box=(30.0, 30.0, 30.0), H=H, DT=0.1, G=1.0,
+                     interpolation=2, finite_diff=0, greens=2, diameter=3 * H)
+    q = O.P3MConfig(comp_box=(30.0, 30.0, 30.0), cutoff=3 * H, diameter=3 * H, cloud_shape=1)
+    x, vv, esc = O.ref_run(cfg, q, p, v, m, 3)
+    runs["p3m"] = dict(pos=p, vel=v, mass=m, pos_out=x, vel_out=vv, escaped=np.int32(esc),
+                       sim_length=np.int32(3), **_cfg_arrays(cfg), **_p3m_arrays(q))
+    # escape: particles pushed out of the box by a strong external field pointing outwards
+    pe = p.copy()
+    pe[:10, 0] = 29.6
+    ve = v.copy()
+    ve[:10, 0] = 0.05 * 30
+    cfg = O.PMConfig(grid=(32, 32, 32), box=(30.0, 30.0, 30.0), H=H, DT=0.1, G=1.0,
+                     interpolation=1, finite_diff=0, greens=0, diameter=0.0)
+    x, vv, esc = O.ref_run(cfg, None, pe, ve, m, 6)
+    runs["escape"] = dict(pos=pe, vel=ve, mass=m, pos_out=x, vel_out=vv, escaped=np.int32(esc),
+                          sim_length=np.int32(6), **_cfg_arrays(cfg))
+    np.savez_compressed(os.path.join(HERE, "runs.npz"),
+                        **{f"{c}/{k}": a for c, d in runs.items() for k, a in d.items()})
+    # ---- SR force table and FP32 direct sum
+    t = {}
+    for cs in (0, 1):
+        for eps in (0.0, 0.5):
+            qq = O.P3MConfig(comp_box=(30.0,) * 3, cutoff=3 * H, diameter=3 * H, softening=eps,
+                             cloud_shape=cs)
+            t[f"cs{cs}_eps{eps}"] = O.ref_sr_table(qq, H)[0]
+    pp, _, mm = inputs(50, 300, 0.0, 10.0)
+    t["pp_pos"] = pp
+    t["pp_mass"] = mm
+    t["pp_acc"] = O.ref_pp_accel(pp, mm, 1.0, 0.0)
+    np.savez_compressed(os.path.join(HERE, "misc.npz"), **t)
+    print("golden fixtures written to", HERE)
+
+
+def _cfg_arrays(cfg):
+    return dict(grid=np.array(cfg.grid, np.int32), box=np.array(cfg.box, np.float32),
+                HDTG=np.array([cfg.H, cfg.DT, cfg.G], np.float32),
+                scheme=np.array([cfg.interpolation, cfg.finite_diff, cfg.greens], np.int32),
+                diameter=np.float32(cfg.diameter),
+                ext=np.array(cfg.ext if cfg.ext else [np.nan] * 6, np.float32))
+
+
+def _p3m_arrays(q):
+    return dict(comp_box=np.array(q.comp_box, np.float32),
+                cds=np.array([q.cutoff, q.diameter, q.softening], np.float32),
+                flags=np.array([q.cloud_shape, q.use_table, q.y_sorting], np.int32))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,129 @@
+"""GPU parity of the P3M path (chaining mesh + short-range pair pass) through the C ABI.
+
+Cell lists are compared bit for bit with the reference's ChainingMesh (golden fixtures, exact
+y ties and duplicated particles included).  Forces: RMS relative error <= 1e-5 against the FP64
+oracle and against the reference's FP32 result, on small cases and, at the full 262,144-particle
+disk workload, on a 1,500-particle subsample (FP64 PM + brute-force short-range sum).
+"""
+import numpy as np
+import pytest
+
+from conftest import load_npz, rel_rms
+from oracle import oracle as O
+from test_gpu_pm import make_pm
+from test_oracle_pin import cfg_from, p3m_from
+
+pytestmark = pytest.mark.gpu
+
+P3M = load_npz("p3m_forces.npz")
+
+
+def make_p3m(cfg, q, pos, vel, mass):
+    import particlesimulation_gb300 as P
+    pm = make_pm(cfg, pos, vel, mass)
+    p3m = P.P3MMethod(pm, q.comp_box, q.cutoff, q.diameter, cfg.H, q.softening,
+                      P.CloudShape(q.cloud_shape), bool(q.use_table), bool(q.y_sorting))
+    return pm, p3m
+
+
+@pytest.mark.parametrize("case", [c for c in P3M if c != "inputs"])
+def test_p3m_force_matches_reference_and_fp64(gpu_lib, case):
+    d = P3M[case]
+    inp = P3M["inputs"]
+    cfg, q = cfg_from(d), p3m_from(d)
+    pm, p3m = make_p3m(cfg, q, inp["pos"], inp["vel"], inp["mass"])
+    p3m.force()
+    acc = pm.getParticles()[2]
+    f64 = O.port_p3m_accel(cfg, q, inp["pos"], inp["vel"], inp["mass"], prec=1)
+    assert rel_rms(acc, f64) < 1e-5, "vs FP64 oracle"
+    # the direct (table-free) S1/S2 formulas lose ~1.5e-5 to FP32 cancellation in the reference
+    tol = 1e-5 if q.use_table else 3e-5
+    assert rel_rms(acc, d["acc"]) < tol, "vs reference FP32"
+    p3m.close()
+    pm.close()
+
+
+@pytest.mark.parametrize("ys", [1, 0])
+def test_cell_lists_bit_exact(gpu_lib, ys):
+    d = load_npz("cell_lists.npz")
+    H = float(d["H"])
+    pc = d["pos_code"]
+    n = len(pc)
+    q = O.P3MConfig(comp_box=tuple(float(b) for b in d["q"]["comp_box"]),
+                    cutoff=float(d["q"]["cds"][0]), diameter=float(d["q"]["cds"][1]),
+                    cloud_shape=1, y_sorting=ys)
+    cfg = O.PMConfig(grid=(32, 32, 32), box=(30.0,) * 3, H=H, DT=0.1, G=1.0, interpolation=2,
+                     finite_diff=0, greens=0)
+    pm, p3m = make_p3m(cfg, q, pc * np.float32(H), np.zeros_like(pc), np.full(n, 1.0 / n, np.float32))
+    pm.setParticles(pc, np.zeros_like(pc), units="code")  # the fixture's code-unit positions
+    p3m.force()
+    order, counts, dims = p3m.getCellLists()
+    assert dims == tuple(d[f"y{ys}"]["dims"])
+    np.testing.assert_array_equal(counts, d[f"y{ys}"]["counts"])
+    np.testing.assert_array_equal(order, d[f"y{ys}"]["order"])
+    # twice in a row (the particles are now in sorted order: ties must still go by index)
+    p3m.force()
+    order2, counts2, _ = p3m.getCellLists()
+    np.testing.assert_array_equal(order2, d[f"y{ys}"]["order"])
+    p3m.close()
+    pm.close()
+
+
+def test_sr_table_matches_reference(gpu_lib):
+    d = load_npz("misc.npz")
+    H = 30.0 / 16
+    for cs in (0, 1):
+        for eps in (0.0, 0.5):
+            q = O.P3MConfig(comp_box=(30.0,) * 3, cutoff=3 * H, diameter=3 * H, softening=eps,
+                            cloud_shape=cs)
+            cfg = O.PMConfig(grid=(32, 32, 32), box=(30.0,) * 3, H=H)
+            p = np.full((2, 3), 15.0, np.float32)
+            pm, p3m = make_p3m(cfg, q, p, p * 0, np.ones(2, np.float32))
+            t, _ = p3m.getSRForceTable()
+            np.testing.assert_allclose(t, d[f"cs{cs}_eps{eps}"], rtol=2e-6, atol=0)
+            p3m.close()
+            pm.close()
+
+
+def test_p3m_run_matches_reference_run(gpu_lib):
+    d = load_npz("runs.npz")["p3m"]
+    cfg, q = cfg_from(d), p3m_from(d)
+    pm, p3m = make_p3m(cfg, q, d["pos"], d["vel"], d["mass"])
+    escaped, steps = p3m.run(int(d["sim_length"]))
+    assert not escaped and steps == int(d["sim_length"]) + 1
+    x, v, _ = pm.getParticles(units="original")
+    assert np.abs(x - d["pos_out"]).max() < 2e-6 * np.abs(d["pos_out"]).max()
+    assert rel_rms(v, d["vel_out"]) < 1e-5
+    p3m.close()
+    pm.close()
+
+
+def test_p3m_full_size_disk(gpu_lib):
+    """The 262,144-particle disk + bulge workload (128^3, TSC, S2, cutoff 3H): size-independent
+    properties of the cell lists on the whole system, forces on a subsample vs FP64."""
+    from particlesimulation_gb300 import workloads as W
+    w = W.disk_p3m()
+    cfg = O.PMConfig(grid=w.grid, box=w.box, H=w.H, DT=w.DT, G=w.G, interpolation=w.interpolation,
+                     finite_diff=w.finite_diff, greens=w.greens, diameter=w.diameter)
+    q = O.P3MConfig(comp_box=w.p3m["comp_box"], cutoff=w.p3m["cutoff"], diameter=w.p3m["diameter"],
+                    softening=0.0, cloud_shape=1)
+    pm, p3m = make_p3m(cfg, q, w.pos, w.vel, w.mass)
+    p3m.force()
+    acc = pm.getParticles()[2]
+    order, counts, dims = p3m.getCellLists()
+    # cell lists: a permutation of the particles inside the mesh, grouped by cell, y ascending,
+    # ties by index
+    xc = (w.pos / np.float32(w.H)).astype(np.float32)
+    HC = np.float32(np.float32(w.box[0] / dims[0]) / np.float32(w.H))
+    cell = (xc / HC).astype(np.int64)
+    flat = cell[:, 0] + cell[:, 1] * dims[0] + cell[:, 2] * dims[0] * dims[1]
+    expect = np.lexsort((np.arange(w.n), xc[:, 1], flat))
+    np.testing.assert_array_equal(order, expect)
+    np.testing.assert_array_equal(counts, np.bincount(flat, minlength=int(np.prod(dims))))
+    # forces on a subsample vs FP64 (PM for all + brute-force short range for the targets)
+    rng = np.random.default_rng(0)
+    idx = np.sort(rng.choice(w.n, 1500, replace=False)).astype(np.int32)
+    f64 = O.port_p3m_accel_targets(cfg, q, w.pos, w.vel, w.mass, idx, prec=1)
+    assert rel_rms(acc[idx], f64) < 1e-5
+    p3m.close()
+    pm.close()
