@@ -1,0 +1,350 @@
+#!/usr/bin/env python3
+"""P3M force-and-step throughput (particle-steps/s) on GB300.
+
+Workload (default): the 262,144-particle exponential disk + Plummer bulge, 128^3 mesh, TSC,
+S2-shaped particles, plain P3M with a 3-mesh-cell cutoff on the y-sorted chaining mesh,
+dt = 0.005 (particlesimulation_gb300.workloads.disk_p3m).  A step is one iteration of the
+reference's run loop: drift, P3M force (cell lists, deposit, FFT Poisson solve, interpolation,
+short-range pair pass), kick.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+ours:       inputs resident on the device; W warm-up steps, then K steps, each timed with CUDA
+            events on the handle's stream (pmgb_pm_advance), L2 flushed (256 MB write) before
+            every step; max over ranks.  Replicas only: every rank runs its own copy of the
+            system (a single P3M system does not shard), so the whole-job value is N times the
+            per-rank particle count over the slowest rank's time.
+            e2e: the same steps through the C ABI with host buffers: per step the state is
+            copied host->device from pinned memory (pmgb_pm_set_particles), advanced, and read
+            back device->host (pmgb_pm_get_particles).
+reference:  the reference's CPU P3M path (the oracle port of it: oracle/port.cpp, float, all
+            host threads) on the same workload; each step a bounded sample (see cpu_sample()).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s on 1 GB300: plain P3M vs learned closure at equal force error"
+UNIT = "particle-steps/s"
+L2_FLUSH_BYTES = 256 << 20
+PAIR_STRIDE = 64  # CPU sample: every 64th i-particle of the pair pass (j loops complete)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="disk_p3m")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-forces", type=int, default=0, metavar="K",
+                    help="only run K force evaluations of the workload and print the stage "
+                         "times (the command profiled with ncu)")
+    return ap.parse_args()
+
+
+def run_profile_forces(args):
+    from particlesimulation_gb300 import workloads as W
+    w = W.WORKLOADS[args.workload]()
+    pm, p3m = make_system(w)
+    for _ in range(args.profile_forces):
+        (p3m.force() if p3m else pm.pmMethodStep())
+    out = {"stage_ms": pm.stageTimes()}
+    if p3m:
+        out["ordered_pairs"] = p3m.pairCount()
+        p3m.close()
+    pm.close()
+    print(json.dumps(out))
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def config_of(w):
+    d = dict(workload=f"{w.name}: {w.n:,} particles, {w.grid[0]}^3 mesh, "
+                      f"{['NGP', 'CIC', 'TSC'][w.interpolation]}, "
+                      + (f"P3M cutoff {w.p3m['cutoff'] / w.H:g} mesh cells" if w.p3m else "PM"),
+             particles=w.n, mesh=list(w.grid), dt=w.DT, method="P3M" if w.p3m else "PM",
+             parallelism="replicas")
+    return d
+
+
+def load_peaks():
+    for p in (os.path.join(ROOT, "MEASURED_PEAKS.json"),):
+        if os.path.exists(p):
+            with open(p) as f:
+                return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms while running."""
+
+    def __init__(self, gpu_id: str):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", self.gpu_id, f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.1)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.close()
+        rows = []
+        with open(self.f.name) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) == 7 and parts[0].replace(".", "").isdigit():
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(float(r[0]) for r in rows),
+                "sm_max_mhz": max(float(r[1]) for r in rows),
+                "power_w_max": max(float(r[2]) for r in rows if r[2].replace(".", "").isdigit()),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_sample(w, threads, steps=1):
+    """The reference's CPU P3M step on the full workload, sampled: the PM part and the y-sorted
+    chaining-mesh build run on all particles, the short-range pair pass on every PAIR_STRIDE-th
+    i-particle of each cell list (complete j loops) and is scaled by PAIR_STRIDE.  Returns
+    (particle-steps/s, seconds per step, breakdown)."""
+    from oracle import oracle as O
+    cfg = O.PMConfig(grid=w.grid, box=w.box, H=w.H, DT=w.DT, G=w.G, interpolation=w.interpolation,
+                     finite_diff=w.finite_diff, greens=w.greens, diameter=w.diameter,
+                     periodic=int(w.periodic))
+    q = None
+    if w.p3m:
+        q = O.P3MConfig(comp_box=w.p3m["comp_box"], cutoff=w.p3m["cutoff"],
+                        diameter=w.p3m["diameter"], softening=w.p3m["softening"],
+                        cloud_shape=w.p3m["cloud_shape"], use_table=w.p3m["table"],
+                        y_sorting=w.p3m["ysort"])
+    r = O.port_time_steps(cfg, q, w.pos, w.vel, w.mass, steps, threads, PAIR_STRIDE if q else 1)
+    return w.n / r["est"], r["est"], r
+
+
+def sample_text(w):
+    return (f"{w.name}, all {w.n:,} particles: PM step and chaining-mesh build in full, short-range "
+            f"pair pass for every {PAIR_STRIDE}th i-particle (full j loops) scaled by {PAIR_STRIDE}; "
+            "oracle port of the reference's CPU P3M in float")
+
+
+def make_system(w):
+    import particlesimulation_gb300 as P
+    pm = P.PMMethod(w.state, w.mass, w.box, None, w.H, w.DT, w.G,
+                    P.InterpolationScheme(w.interpolation), P.FiniteDiffScheme(w.finite_diff),
+                    P.GreensFunction(w.greens), w.diameter, w.grid, periodic=w.periodic)
+    p3m = None
+    if w.p3m:
+        q = w.p3m
+        p3m = P.P3MMethod(pm, q["comp_box"], q["cutoff"], q["diameter"], w.H, q["softening"],
+                          P.CloudShape(q["cloud_shape"]), bool(q["table"]), bool(q["ysort"]))
+    return pm, p3m
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import particlesimulation_gb300 as P
+    from particlesimulation_gb300 import workloads as W
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    w = W.WORKLOADS[args.workload]()
+    pm, p3m = make_system(w)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    def flush_l2():
+        flush.random_(0, 255)
+        torch.cuda.synchronize()
+
+    escaped, _ = pm.run(0)  # initial force, half kick, first iteration (state ready for advance)
+    if escaped:
+        raise RuntimeError("a particle left the box during set-up")
+    for _ in range(args.warmup):
+        flush_l2()
+        pm.advance(1)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    props = torch.cuda.get_device_properties(local)
+    uuid = getattr(props, "uuid", None)
+    clocks = ClockSampler(f"GPU-{uuid}" if uuid is not None else str(local))
+    launches0 = pm.kernelLaunches()
+    clocks.start()
+    total_ms = 0.0
+    for _ in range(args.steps):
+        flush_l2()
+        esc, done, ms = pm.advance(1)
+        if esc:
+            raise RuntimeError("a particle left the box during the timed steps")
+        total_ms += ms
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = pm.kernelLaunches() - launches0
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+        total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    value = world * w.n * args.steps / (total_ms * 1e-3)
+
+    # ---- roofline of the dominant kernel (the short-range pair pass): FP32 issue bound
+    stage = {}
+    pair_ms, pairs = [], []
+    for _ in range(3):
+        flush_l2()
+        (p3m.force() if p3m else pm.pmMethodStep())
+        stage = pm.stageTimes()
+        pair_ms.append(stage["pair"])
+        if p3m:
+            pairs.append(p3m.pairCount())
+    peaks, peak_src = load_peaks()
+    fp32_peak = P.methods.fp32_peak_tflops()
+    roofline = None
+    if p3m:
+        flop = 20.0 * (statistics.median(pairs) / 2.0)  # 20 FLOP per unordered pair in range
+        t = statistics.median(pair_ms) * 1e-3
+        achieved = flop / t / 1e12
+        traffic = None  # dram read + write bytes of one launch, from the committed ncu summary
+        prof = os.path.join(ROOT, "profiles", f"pair_kernel_{w.name}.md")
+        if os.path.exists(prof):
+            with open(prof) as f:
+                for line in f:
+                    if line.startswith("dram_bytes_per_launch:"):
+                        traffic = float(line.split(":", 1)[1].split()[0])
+        roofline = {"kernel": "pair_kernel", "bound": "fp32", "achieved": round(achieved, 3),
+                    "peak": round(fp32_peak, 3), "unit": "TFLOP/s",
+                    "frac": round(achieved / fp32_peak, 4), "traffic": traffic,
+                    "peak_source": "FP32 FMA probe measured in this run (pmgb_fp32_peak_probe); "
+                                   "the pair pass is CUDA-core FP32 bound, not HBM or tensor",
+                    "flop_per_launch": flop, "pairs_in_range_unordered": statistics.median(pairs) / 2,
+                    "launch_ms": round(statistics.median(pair_ms), 4)}
+    # ---- HBM roofline of the PM stages (deposit + Poisson solve + interpolation)
+    pm_ms = stage["deposit"] + stage["poisson"] + stage["interpolation"]
+    pm_bytes = 60.0 * w.n + 26.0 * float(np.prod(w.grid))
+    roofline_pm = {"bound": "hbm", "achieved": round(pm_bytes / (pm_ms * 1e-3) / 1e9, 1),
+                   "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                   "frac": round(pm_bytes / (pm_ms * 1e-3) / 1e9 / peaks.get("hbm_gbs"), 4),
+                   "bytes_per_step": pm_bytes, "stage_ms": {k: round(v, 4) for k, v in stage.items()},
+                   "peak_source": peak_src}
+
+    # ---- e2e through the C ABI with pinned host buffers
+    pos_h = torch.empty((w.n, 3), dtype=torch.float32, pin_memory=True).numpy()
+    vel_h = torch.empty((w.n, 3), dtype=torch.float32, pin_memory=True).numpy()
+    acc_h = torch.empty((w.n, 3), dtype=torch.float32, pin_memory=True).numpy()
+    pm.getParticles(units="original", pos=pos_h, vel=vel_h, acc=acc_h)
+    k_e2e = args.steps
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(k_e2e):
+        pm.setParticles(pos_h, vel_h, units="original")
+        pm.advance(1)
+        pm.getParticles(units="original", pos=pos_h, vel=vel_h, acc=acc_h)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * w.n * k_e2e / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(pos_h.nbytes + vel_h.nbytes),
+           "d2h_bytes_per_step": int(pos_h.nbytes + vel_h.nbytes + acc_h.nbytes)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count()
+        v, sec, r = cpu_sample(w, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": sample_text(w), "seconds_per_step": sec,
+               "breakdown_s": {k: round(float(x), 4) for k, x in r.items()}}
+    if p3m:
+        p3m.close()
+    pm.close()
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded generator, particlesimulation_gb300/workloads.py)",
+                "config": {**config_of(w), "l2": "256 MB L2 flush before every timed step"},
+                "e2e": e2e, "roofline": roofline, "roofline_pm": roofline_pm,
+                "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+                "impl": "ours"}
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from particlesimulation_gb300 import workloads as W
+    w = W.WORKLOADS[args.workload]()
+    threads = os.cpu_count()
+    for _ in range(min(args.warmup, 1)):  # a CPU path has no warm-up effect beyond first touch
+        cpu_sample(w, threads)
+    secs = []
+    for _ in range(args.steps):
+        _, sec, _ = cpu_sample(w, threads)
+        secs.append(sec)
+    total = sum(secs)
+    value = w.n * args.steps / total
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator, particlesimulation_gb300/workloads.py)",
+            "config": config_of(w), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample_text(w)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.profile_forces:
+        run_profile_forces(args)
+    elif args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

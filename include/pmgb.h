@@ -183,8 +183,18 @@ int pmgb_p3m_get_cell_lists(pmgb_p3m* p3m, int* order, int* counts, int* dims3);
  * its r^2 spacing, code units. */
 int pmgb_p3m_get_sr_table(pmgb_p3m* p3m, float* table500, float* delta_sq);
 
+/* Ordered particle pairs (i, j), i != j, closer than the cutoff in the last force evaluation
+ * (each unordered pair counts twice).  No reference counterpart: it sizes the pair pass's
+ * FLOP count (20 FLOP per unordered pair). */
+int pmgb_p3m_pair_count(pmgb_p3m* p3m, unsigned long long* ordered_pairs);
+
 /* ---------------------------------------------------------------- misc -------------- */
+/* FP32 FMA throughput of the current device in TFLOP/s, measured by a timed FMA kernel (the
+ * roofline denominator of the FP32-bound pair pass).  No reference counterpart. */
+int pmgb_fp32_peak_probe(float* tflops);
 const char* pmgb_last_error(void);
+/* Number of kernels this process has launched through the library. */
+int pmgb_kernel_launches(long long* count);
 /* Library build identification (architecture string). */
 const char* pmgb_version(void);
 

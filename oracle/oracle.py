@@ -315,12 +315,14 @@ def port_sr_table(q: P3MConfig, H):
     return t, d2.value
 
 
-def port_time_steps(cfg: PMConfig, q: P3MConfig | None, pos, vel, mass, steps, nthreads):
+def port_time_steps(cfg: PMConfig, q: P3MConfig | None, pos, vel, mass, steps, nthreads,
+                    pair_stride=1):
+    """Seconds per step of the port in float: dict(est, pm, cells, pair_sampled)."""
     n = len(mass)
     st, m = _state(pos, vel), _f32(mass)
-    sec = C.c_double(0)
+    out = np.zeros(4, np.float64)
     rc = port().port_time_steps(C.byref(cfg.c()), C.byref(q.c()) if q is not None else None, n,
                                 _ptr(st, C.c_float), _ptr(m, C.c_float), steps, nthreads,
-                                C.byref(sec))
+                                pair_stride, _ptr(out, C.c_double))
     assert rc == 0
-    return sec.value
+    return dict(est=out[0], pm=out[1], cells=out[2], pair_sampled=out[3])

@@ -103,11 +103,12 @@ int port_p3m_accel_targets(int prec, const orc_pm_params* p, const orc_p3m_param
                            double* acc, int nthreads);
 /* The SR force table of P3MMethod::initSRForceTable (p3mMethod.cpp:275-294), float. */
 int port_sr_table(const orc_p3m_params* q, float H, float* table /*500*/, float* delta_sq);
-/* Times `steps` force-and-step iterations of the port's P3M (or PM if q == NULL) in float,
- * after the initial solve.  Returns seconds per step in *sec_per_step. */
+/* Times `steps` run-loop iterations (drift, force, kick) of the port in float on nthreads host
+ * threads; pair_stride S > 1 samples every S-th i-particle of the pair pass and scales its time.
+ * out4 = {est. seconds per full step, PM s, cell-list s, sampled pair s} per step. */
 int port_time_steps(const orc_pm_params* p, const orc_p3m_params* q, int n,
                     const float* state, const float* masses, int steps, int nthreads,
-                    double* sec_per_step);
+                    int pair_stride, double* out4);
 
 #ifdef __cplusplus
 }

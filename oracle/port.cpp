@@ -615,6 +615,7 @@ struct P3M {
     T F = mi * mj * (table[t] + (ksi - t) * (table[t + 1] - table[t]));
     return F * rij;
   }
+  int pairStride = 1;  // timing samples: only every pairStride-th particle of a list is an i
   void threadJob(int tid, int threads) {
     const auto& x = pm.x;
     const auto& m = pm.m;
@@ -624,7 +625,9 @@ struct P3M {
       for (int s = 0; s < 14; ++s) {
         int cn = nb[s];
         if (cn < 0) continue;
-        for (int i = cm.hoc[c]; i >= 0; i = cm.next[i]) {
+        int ipos = 0;
+        for (int i = cm.hoc[c]; i >= 0; i = cm.next[i], ++ipos) {
+          if (pairStride > 1 && ipos % pairStride) continue;
           for (int j = cm.hoc[cn]; j >= 0; j = cm.next[j]) {
             if (q.y_sorting && x[j].y - x[i].y > re) break;
             if (i == j) continue;
@@ -643,12 +646,17 @@ struct P3M {
       sr[i] = {};
       for (auto& s : slot[i]) s = {};
     }
+    auto t0 = std::chrono::steady_clock::now();
     cm.fill(pm.x, q.y_sorting != 0);
+    auto t1 = std::chrono::steady_clock::now();
+    fillSec += std::chrono::duration<double>(t1 - t0).count();
     int th = std::max(1, nthreads);
     std::vector<std::thread> ts;
     for (int t = 0; t < th; ++t) ts.emplace_back(&P3M::threadJob, this, t, th);
     for (auto& t : ts) t.join();
+    pairSec += std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
   }
+  double fillSec = 0, pairSec = 0;
   void correct() {  // correctAccelerations (p3mMethod.cpp:50-57)
     for (int i = 0; i < pm.N; ++i) {
       V3<T> tot{};
@@ -907,31 +915,40 @@ int port_sr_table(const orc_p3m_params* q, float H, float* table, float* delta_s
 }
 
 int port_time_steps(const orc_pm_params* p, const orc_p3m_params* q, int n, const float* state,
-                    const float* masses, int steps, int nthreads, double* sec_per_step) {
+                    const float* masses, int steps, int nthreads, int pair_stride, double* out4) {
+  // Times `steps` iterations of the run loop body (drift, force, kick) in float with nthreads
+  // host threads.  With pair_stride S > 1 only every S-th particle of each cell list is an
+  // i-particle of the pair pass (its j loops are complete), and the pair time is scaled by S.
+  // out4 = {estimated seconds per full step, PM seconds, cell-list seconds, pair seconds as
+  // measured (sampled)}, all per step.
   PM<float> pm(p, n, state, masses, nthreads);
   std::unique_ptr<P3M<float>> p3m;
-  if (q) p3m = std::make_unique<P3M<float>>(q, pm, nthreads);
+  if (q) {
+    p3m = std::make_unique<P3M<float>>(q, pm, nthreads);
+    p3m->pairStride = std::max(1, pair_stride);
+  }
   pm.toCode();
   pm.initGreen();
-  auto force = [&]() {
-    pm.step();
-    if (p3m) {
-      p3m->shortRange();
-      p3m->correct();
-    }
-  };
-  force();
-  for (int i = 0; i < n; ++i) pm.v[i] += 0.5f * pm.a[i];
-  auto t0 = std::chrono::steady_clock::now();
+  double pmSec = 0;
   for (int t = 0; t < steps; ++t) {
     for (int i = 0; i < n; ++i) pm.x[i] += pm.v[i];
     pm.statesToOriginal();
     pm.statesToCode();
-    force();
+    auto t0 = std::chrono::steady_clock::now();
+    pm.step();
+    pmSec += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (p3m) {
+      p3m->shortRange();
+      p3m->correct();
+    }
     for (int i = 0; i < n; ++i) pm.v[i] += pm.a[i];
   }
-  auto t1 = std::chrono::steady_clock::now();
-  *sec_per_step = std::chrono::duration<double>(t1 - t0).count() / std::max(1, steps);
+  const int k = std::max(1, steps);
+  const double fill = p3m ? p3m->fillSec / k : 0.0, pair = p3m ? p3m->pairSec / k : 0.0;
+  out4[1] = pmSec / k;
+  out4[2] = fill;
+  out4[3] = pair;
+  out4[0] = out4[1] + fill + pair * (p3m ? p3m->pairStride : 1);
   return 0;
 }
 

@@ -20,6 +20,7 @@ EXPORTS = [
     "pmgb_pm_get_density", "pmgb_pm_get_potential", "pmgb_pm_get_greens_function",
     "pmgb_pm_stage_times", "pmgb_pm_size", "pmgb_p3m_create", "pmgb_p3m_destroy",
     "pmgb_p3m_force", "pmgb_p3m_run", "pmgb_p3m_get_cell_lists", "pmgb_p3m_get_sr_table",
+    "pmgb_p3m_pair_count", "pmgb_fp32_peak_probe", "pmgb_kernel_launches",
     "pmgb_last_error", "pmgb_version",
 ]
 
@@ -81,6 +82,9 @@ def lib() -> C.CDLL:
         L.pmgb_p3m_run.argtypes = [vp, C.c_int, ip]
         L.pmgb_p3m_get_cell_lists.argtypes = [vp, ip, ip, ip]
         L.pmgb_p3m_get_sr_table.argtypes = [vp, fp, fp]
+        L.pmgb_p3m_pair_count.argtypes = [vp, C.POINTER(C.c_ulonglong)]
+        L.pmgb_fp32_peak_probe.argtypes = [fp]
+        L.pmgb_kernel_launches.argtypes = [C.POINTER(C.c_longlong)]
         L.pmgb_last_error.restype = C.c_char_p
         L.pmgb_version.restype = C.c_char_p
         _lib = L

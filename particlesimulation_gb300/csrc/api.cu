@@ -11,6 +11,7 @@
 // A pmgb_p3m adds the chaining mesh (cell starts, work items) and the short-range table, and
 // makes every force evaluation of its PM handle a P3M one.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -54,10 +55,13 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
                 int Mx, int My, int Mz, u32* item_cnt, u32* item_off, u32* nitems, int2* items,
                 u32* counter, const PairParams& pp, const float* table, const StepParams& sp,
                 float kick, int drift, int kdk, float4* pm_out, float4* vi_out, float4* acc_out,
-                unsigned long long* npairs, int* stop, int num_sms, cudaStream_t st);
+                unsigned long long* npairs, int* stop, int num_sms, cudaEvent_t ev_pair,
+                cudaStream_t st);
 
 static thread_local std::string g_last_error;
 void set_error(const std::string& msg) { g_last_error = msg; }
+static std::atomic<long long> g_launches{0};
+void count_launches(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 
 static int ilog2(int v) {
   int l = 0;
@@ -252,11 +256,12 @@ int force(pmgb_pm* h, int kdk, float kick, int drift, int tag, bool timed) {
   }
   rc = launch_interp(false, h->pm[h->cur], h->vi[h->cur], h->acc_pm, n, h->phi, sp, kick, drift, stop, h->st);
   if (rc) return rc;
-  if (timed) cudaEventRecord(h->ev[4], h->st);
+  // ev[4] is recorded just before the pair kernel (after its work-item setup)
   rc = launch_pair(h->pm[h->cur], h->vi[h->cur], h->acc_pm, q->cell_start, q->cd.Mx, q->cd.My, q->cd.Mz,
                    q->item_cnt, q->item_off, q->nitems, q->items, q->counter, q->pp, q->table, sp,
-                   kick, drift, kdk, h->pm[1 - h->cur], h->vi[1 - h->cur], h->acc, q->npairs, stop,
-                   h->num_sms, h->st);
+                   kick, drift, kdk, h->pm[1 - h->cur], h->vi[1 - h->cur], h->acc,
+                   timed ? q->npairs : nullptr, stop,
+                   h->num_sms, timed ? h->ev[4] : nullptr, h->st);
   if (rc) return rc;
   if (kdk) {
     h->cur = 1 - h->cur;
@@ -295,6 +300,12 @@ extern "C" {
 
 const char* pmgb_last_error(void) { return g_last_error.c_str(); }
 const char* pmgb_version(void) { return "pmgb 0.1 sm_103a"; }
+
+int pmgb_kernel_launches(long long* count) {
+  if (!count) return set_error("null argument"), PMGB_EINVAL;
+  *count = g_launches.load();
+  return PMGB_OK;
+}
 
 int pmgb_pm_create(const pmgb_pm_config* cfg, int n, const float* state, const float* masses,
                    pmgb_pm** out) {
@@ -702,6 +713,13 @@ int pmgb_p3m_get_cell_lists(pmgb_p3m* q, int* order, int* counts, int* dims3) {
     const int inside = cs[q->ncells];
     for (int k = 0; k < inside; ++k) std::memcpy(&order[k], &hv[k].w, 4);
   }
+  return PMGB_OK;
+}
+
+int pmgb_p3m_pair_count(pmgb_p3m* q, unsigned long long* ordered_pairs) {
+  if (!q || !ordered_pairs) return set_error("null argument"), PMGB_EINVAL;
+  PMGB_CUDA_TRY(cudaMemcpyAsync(ordered_pairs, q->npairs, sizeof(unsigned long long), cudaMemcpyDeviceToHost, q->pm->st));
+  PMGB_CUDA_TRY(cudaStreamSynchronize(q->pm->st));
   return PMGB_OK;
 }
 

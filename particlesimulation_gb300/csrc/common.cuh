@@ -14,6 +14,8 @@ typedef unsigned int u32;
 
 // ---------------------------------------------------------------- error plumbing ----
 void set_error(const std::string& msg);
+// Host-side tally of kernels launched through this library (pmgb_kernel_launches).
+void count_launches(int k);
 #define PMGB_CUDA_TRY(expr)                                                        \
   do {                                                                             \
     cudaError_t _e = (expr);                                                       \

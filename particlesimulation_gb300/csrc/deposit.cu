@@ -172,6 +172,7 @@ int launch_deposit(int is, const float4* pm, int n, MeshDims m, float scale, u64
   else
     deposit_kernel<2><<<blocks, DEP_THREADS, 0, st>>>(pm, n, m, scale, rho, stop);
   PMGB_LAUNCH_CHECK();
+  count_launches(1);
   return PMGB_OK;
 }
 

@@ -250,6 +250,7 @@ int launch_poisson(u64* rho, float2* spec, float* phi, const float* ghat, const 
   fft_cols_kernel<<<dim3(ctiles, m.nz), FFT_THREADS, ysmem, st>>>(spec, m, 1, 1, nullptr, tw, nmax, stop);
   fft_x_c2r_kernel<<<xblocks, FFT_THREADS, xsmem, st>>>(spec, phi, m, pairs, tw, nmax, stop);
   PMGB_LAUNCH_CHECK();
+  count_launches(5);
   return PMGB_OK;
 }
 

@@ -127,6 +127,7 @@ int launch_green(float* ghat, MeshDims m, int gf, int is, int fds, double a, cud
   const int cs = gf == PMGB_S1_OPTIMAL ? 0 : 1;
   green_kernel<<<152 * 8, 256, 0, st>>>(ghat, m, gf, is, fds, cs, a);
   PMGB_LAUNCH_CHECK();
+  count_launches(1);
   return PMGB_OK;
 }
 

@@ -145,6 +145,7 @@ int launch_interp(bool kdk, float4* pm, float4* vi, float4* acc, int n, const fl
     default: launch_interp_t<2, 1>(kdk, pm, vi, acc, n, phi, sp, kick, drift, stop, st); break;
   }
   PMGB_LAUNCH_CHECK();
+  count_launches(1);
   return PMGB_OK;
 }
 
@@ -167,6 +168,7 @@ int launch_kick_drift(float4* pm, float4* vi, const float4* acc, int n, const St
   if (n <= 0) return PMGB_OK;
   kick_drift_kernel<<<(n + 255) / 256, 256, 0, st>>>(pm, vi, acc, n, sp, kick, drift, stop);
   PMGB_LAUNCH_CHECK();
+  count_launches(1);
   return PMGB_OK;
 }
 

@@ -66,6 +66,7 @@ int launch_unpack(const float4* pm, const float4* vi, const float4* acc, int n, 
   if (n <= 0) return PMGB_OK;
   unpack_kernel<<<(n + 255) / 256, 256, 0, st>>>(pm, vi, acc, n, H, DT, orig, pos, vel, aout);
   PMGB_LAUNCH_CHECK();
+  count_launches(1);
   return PMGB_OK;
 }
 
@@ -74,6 +75,7 @@ int launch_pack(const float* pos, const float* vel, const float* mass_code, int 
   if (n <= 0) return PMGB_OK;
   pack_kernel<<<(n + 255) / 256, 256, 0, st>>>(pos, vel, mass_code, n, H, DT, orig, pm, vi);
   PMGB_LAUNCH_CHECK();
+  count_launches(1);
   return PMGB_OK;
 }
 

@@ -82,6 +82,9 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
 }
 
 
+constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23: adding it rounds to an integer
+
+template <bool TABLE, bool COUNT>
 __global__ void __launch_bounds__(PAIR_THREADS) pair_kernel(
     const float4* __restrict__ pm, const float4* __restrict__ vi, const float4* __restrict__ acc_pm,
     const int* __restrict__ cell_start, const int2* __restrict__ items, const u32* __restrict__ nitems_p,
@@ -90,13 +93,16 @@ __global__ void __launch_bounds__(PAIR_THREADS) pair_kernel(
     float4* __restrict__ vi_out, float4* __restrict__ acc_out, unsigned long long* __restrict__ npairs,
     int* stop) {
   if (*stop) return;
+  // (T[t], T[t+1] - T[t]); entry 499 = (T[499], 0) so that t = 499 at the cutoff is in range
   __shared__ float2 tab[500];
-  for (int t = threadIdx.x; t < 499; t += PAIR_THREADS) {
-    const float a = table[t], b = table[t + 1];
+  __shared__ float4 jbuf[PAIR_WARPS][32];
+  for (int t = threadIdx.x; t < 500; t += PAIR_THREADS) {
+    const float a = table[t], b = t < 499 ? table[t + 1] : a;
     tab[t] = make_float2(a, b - a);
   }
   __syncthreads();
   const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
   const u32 nitems = *nitems_p;
   unsigned long long my_pairs = 0;
   for (;;) {
@@ -137,34 +143,40 @@ __global__ void __launch_bounds__(PAIR_THREADS) pair_kernel(
         const int b = __shfl_sync(0xFFFFFFFFu, jb, k);
         const int e = __shfl_sync(0xFFFFFFFFu, je, k);
         for (int j0 = b; j0 < e; j0 += 32) {
+          // stage 32 candidates in this warp's shared buffer; every lane then reads each one
+          // with a broadcast load
           const int jj = j0 + lane;
-          const float4 pj = jj < e ? pm[jj] : make_float4(3.0e30f, 3.0e30f, 3.0e30f, 0.f);
+          jbuf[warp][lane] = jj < e ? pm[jj] : make_float4(3.0e30f, 3.0e30f, 3.0e30f, 0.f);
+          __syncwarp();
           const int cnt = min(32, e - j0);
           float px = 0.f, py = 0.f, pz = 0.f;
+#pragma unroll 4
           for (int s = 0; s < cnt; ++s) {
-            const float qx = __shfl_sync(0xFFFFFFFFu, pj.x, s);
-            const float qy = __shfl_sync(0xFFFFFFFFu, pj.y, s);
-            const float qz = __shfl_sync(0xFFFFFFFFu, pj.z, s);
-            const float qm = __shfl_sync(0xFFFFFFFFu, pj.w, s);
-            const float dx = pi.x - qx, dy = pi.y - qy, dz = pi.z - qz;
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            if (valid && r2 < pp.re2) {
-              float f;
-              if (pp.use_table) {
-                const float xi = r2 * pp.inv_d2;
-                int t = (int)xi;
-                t = min(t, 498);
-                const float2 tv = tab[t];
-                f = qm * (tv.x + (xi - (float)t) * tv.y);
-              } else {
-                f = r2 > 0.f ? qm * direct_f(pp, r2) : 0.f;
-              }
-              px += f * dx;
-              py += f * dy;
-              pz += f * dz;
-              ++my_pairs;
+            const float4 q = jbuf[warp][s];
+            const float dx = pi.x - q.x, dy = pi.y - q.y, dz = pi.z - q.z;
+            const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            float f;
+            if (TABLE) {
+              // t = floor(xi) from the float's mantissa (full-rate ops instead of two
+              // quarter-rate conversions); at an exact integer xi it may give xi - 1 with
+              // frac = 1, the same point of the piecewise-linear table
+              const float xi = fminf(r2, pp.re2) * pp.inv_d2;
+              const float tf = (xi - 0.5f) + kMagic;
+              const int t = __float_as_int(tf) - __float_as_int(kMagic);
+              const float frac = xi - (tf - kMagic);
+              const float2 tv = tab[t];
+              f = fmaf(frac, tv.y, tv.x);
+            } else {
+              f = r2 > 0.f ? direct_f(pp, r2) : 0.f;
             }
+            const bool in = r2 < pp.re2;
+            f = in ? f * q.w : 0.f;
+            px = fmaf(f, dx, px);
+            py = fmaf(f, dy, py);
+            pz = fmaf(f, dz, pz);
+            if (COUNT) my_pairs += (in && r2 > 0.f && valid) ? 1ull : 0ull;
           }
+          __syncwarp();
           kahan_add(sx, cx, px);
           kahan_add(sy, cy, py);
           kahan_add(sz, cz, pz);
@@ -183,7 +195,7 @@ __global__ void __launch_bounds__(PAIR_THREADS) pair_kernel(
       acc_out[i] = make_float4(a.x, a.y, a.z, 0.f);
     }
   }
-  if (npairs) {
+  if (COUNT) {
     for (int o = 16; o > 0; o >>= 1) my_pairs += __shfl_xor_sync(0xFFFFFFFFu, my_pairs, o);
     if (lane == 0 && my_pairs) atomicAdd(npairs, my_pairs);
   }
@@ -215,7 +227,8 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
                 int Mx, int My, int Mz, u32* item_cnt, u32* item_off, u32* nitems, int2* items,
                 u32* counter, const PairParams& pp, const float* table, const StepParams& sp,
                 float kick, int drift, int kdk, float4* pm_out, float4* vi_out, float4* acc_out,
-                unsigned long long* npairs, int* stop, int num_sms, cudaStream_t st) {
+                unsigned long long* npairs, int* stop, int num_sms, cudaEvent_t ev_pair,
+                cudaStream_t st) {
   const int ncells = Mx * My * Mz;
   const int ntot = ncells + 1;  // + the bucket of particles outside the chaining mesh
   item_count_kernel<<<(ntot + 255) / 256, 256, 0, st>>>(cell_start, ntot, item_cnt, stop);
@@ -223,11 +236,22 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
   if (rc) return rc;
   item_build_kernel<<<(ntot + 255) / 256, 256, 0, st>>>(cell_start, item_off, ntot, items, stop);
   PMGB_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(u32), st));
+  if (npairs) PMGB_CUDA_TRY(cudaMemsetAsync(npairs, 0, sizeof(unsigned long long), st));
+  if (ev_pair) PMGB_CUDA_TRY(cudaEventRecord(ev_pair, st));
   ChainDimsP cd{Mx, My, Mz, ncells};
-  pair_kernel<<<num_sms * 8, PAIR_THREADS, 0, st>>>(pm, vi, acc_pm, cell_start, items, nitems,
-                                                    counter, cd, pp, table, sp, kick, drift, kdk,
-                                                    pm_out, vi_out, acc_out, npairs, stop);
+  const dim3 grid(num_sms * 8), block(PAIR_THREADS);
+#define PMGB_PAIR_ARGS pm, vi, acc_pm, cell_start, items, nitems, counter, cd, pp, table, sp, kick, \
+                       drift, kdk, pm_out, vi_out, acc_out, npairs, stop
+  if (pp.use_table) {
+    if (npairs) pair_kernel<true, true><<<grid, block, 0, st>>>(PMGB_PAIR_ARGS);
+    else pair_kernel<true, false><<<grid, block, 0, st>>>(PMGB_PAIR_ARGS);
+  } else {
+    if (npairs) pair_kernel<false, true><<<grid, block, 0, st>>>(PMGB_PAIR_ARGS);
+    else pair_kernel<false, false><<<grid, block, 0, st>>>(PMGB_PAIR_ARGS);
+  }
+#undef PMGB_PAIR_ARGS
   PMGB_LAUNCH_CHECK();
+  count_launches(3);  // item count, item build, pair pass (the scan counts itself)
   return PMGB_OK;
 }
 

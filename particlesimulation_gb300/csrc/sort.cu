@@ -142,6 +142,7 @@ int radix_sort_pairs(u64** keys, u32** vals, u64** keys_alt, u32** vals_alt, u32
     rs_scatter_kernel<<<nb, RS_THREADS, 0, st>>>(*keys, *vals, *keys_alt, *vals_alt, n, shift,
                                                  mask, hist, nb);
     PMGB_LAUNCH_CHECK();
+    count_launches(3);
     u64* tk = *keys;
     *keys = *keys_alt;
     *keys_alt = tk;
@@ -155,6 +156,7 @@ int radix_sort_pairs(u64** keys, u32** vals, u64** keys_alt, u32** vals_alt, u32
 int exclusive_scan(const u32* in, u32* out, int n, u32* total, cudaStream_t st) {
   exclusive_scan_kernel<<<1, 1024, 0, st>>>(in, out, n, total);
   PMGB_LAUNCH_CHECK();
+  count_launches(1);
   return PMGB_OK;
 }
 
@@ -267,6 +269,7 @@ int launch_chain_keys(const float4* pm, const float4* vi, int n, ChainDims c, in
   int ncells = c.Mx * c.My * c.Mz;
   chain_keys_kernel<<<(n + 255) / 256, 256, 0, st>>>(pm, vi, n, c, ysort, ncells, stop, keys, vals);
   PMGB_LAUNCH_CHECK();
+  count_launches(1);
   return PMGB_OK;
 }
 
@@ -274,6 +277,7 @@ int launch_fix_ties(const u64* keys, u32* vals, const float4* vi, int n, const i
                     cudaStream_t st) {
   fix_ties_kernel<<<(n + 255) / 256, 256, 0, st>>>(keys, vals, vi, n, stop);
   PMGB_LAUNCH_CHECK();
+  count_launches(1);
   return PMGB_OK;
 }
 
@@ -281,6 +285,7 @@ int launch_brick_keys(const float4* pm, int n, MeshDims m, int bshift, const int
                       u32* vals, cudaStream_t st) {
   brick_keys_kernel<<<(n + 255) / 256, 256, 0, st>>>(pm, n, m, bshift, stop, keys, vals);
   PMGB_LAUNCH_CHECK();
+  count_launches(1);
   return PMGB_OK;
 }
 
@@ -297,6 +302,7 @@ int launch_gather(const u64* keys, const u32* vals, int n, const float4* pm_in,
   gather_kernel<<<(n + 255) / 256, 256, 0, st>>>(keys, vals, n, pm_in, vi_in, pm_out, vi_out,
                                                  cell_start, ncells_total, stop);
   PMGB_LAUNCH_CHECK();
+  count_launches(1);
   return PMGB_OK;
 }
 

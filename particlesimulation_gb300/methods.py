@@ -146,12 +146,16 @@ class PMMethod:
         rc = check(lib().pmgb_pm_advance(self._h, int(nSteps), C.byref(done), C.byref(ms)))
         return rc == _lib.PMGB_EESCAPED, done.value, ms.value
 
-    def getParticles(self, units: str = "code"):
-        """(positions, velocities, accelerations), each (N, 3) float32 in original index order."""
+    def getParticles(self, units: str = "code", pos=None, vel=None, acc=None):
+        """(positions, velocities, accelerations), each (N, 3) float32 in original index order.
+        Caller-provided (e.g. pinned) float32 output arrays are filled in place."""
         n = self.N
-        pos = np.zeros((n, 3), np.float32)
-        vel = np.zeros((n, 3), np.float32)
-        acc = np.zeros((n, 3), np.float32)
+        pos = np.zeros((n, 3), np.float32) if pos is None else pos
+        vel = np.zeros((n, 3), np.float32) if vel is None else vel
+        acc = np.zeros((n, 3), np.float32) if acc is None else acc
+        for a in (pos, vel, acc):
+            if a.dtype != np.float32 or not a.flags.c_contiguous or a.size != 3 * n:
+                raise ValueError("output arrays must be contiguous float32 of shape (N, 3)")
         u = UNITS_ORIGINAL if units == "original" else UNITS_CODE
         check(lib().pmgb_pm_get_particles(self._h, _fp(pos), _fp(vel), _fp(acc), u))
         return pos, vel, acc
@@ -160,6 +164,12 @@ class PMMethod:
         n = self.N
         u = UNITS_ORIGINAL if units == "original" else UNITS_CODE
         check(lib().pmgb_pm_set_particles(self._h, _fp(_f32(pos, (n, 3))), _fp(_f32(vel, (n, 3))), u))
+
+    def kernelLaunches(self) -> int:
+        """Kernels this process has launched through the library so far."""
+        c = C.c_longlong(0)
+        check(lib().pmgb_kernel_launches(C.byref(c)))
+        return int(c.value)
 
     def escapedComputationalBox(self) -> bool:
         e = C.c_int(0)
@@ -189,6 +199,13 @@ class PMMethod:
         t = np.zeros(5, np.float32)
         check(lib().pmgb_pm_stage_times(self._h, _fp(t)))
         return dict(zip(["sort", "deposit", "poisson", "interpolation", "pair"], t.tolist()))
+
+
+def fp32_peak_tflops() -> float:
+    """Measured FP32 FMA throughput of the current GPU (TFLOP/s)."""
+    t = C.c_float(0)
+    check(lib().pmgb_fp32_peak_probe(C.byref(t)))
+    return float(t.value)
 
 
 class P3MMethod:
@@ -246,6 +263,15 @@ class P3MMethod:
         check(lib().pmgb_p3m_get_cell_lists(self._h, order.ctypes.data_as(ip),
                                             counts.ctypes.data_as(ip), dims))
         return order[: counts.sum()], counts, (mx, my, mz)
+
+    def advance(self, nSteps: int):
+        return self.pm.advance(nSteps)
+
+    def pairCount(self) -> int:
+        """Ordered pairs within the cutoff in the last force evaluation."""
+        c = C.c_ulonglong(0)
+        check(lib().pmgb_p3m_pair_count(self._h, C.byref(c)))
+        return int(c.value)
 
     def getSRForceTable(self):
         t = np.zeros(500, np.float32)
