@@ -48,6 +48,10 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="disk_p3m")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-closure", action="store_true",
+                    help="skip the plain-P3M vs learned-closure comparison")
+    ap.add_argument("--closure-epochs", type=int, default=8)
+    ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--profile-forces", type=int, default=0, metavar="K",
                     help="only run K force evaluations of the workload and print the stage "
                          "times (the command profiled with ncu)")
@@ -62,6 +66,8 @@ def run_profile_forces(args):
         (p3m.force() if p3m else pm.pmMethodStep())
     out = {"stage_ms": pm.stageTimes()}
     if p3m:
+        p3m.setPairCounting(True)
+        p3m.force()
         out["ordered_pairs"] = p3m.pairCount()
         p3m.close()
     pm.close()
@@ -227,13 +233,16 @@ def run_ours(args):
     # ---- roofline of the dominant kernel (the short-range pair pass): FP32 issue bound
     stage = {}
     pair_ms, pairs = [], []
+    if p3m:  # one evaluation with the in-range pair counter, timing without it
+        p3m.setPairCounting(True)
+        p3m.force()
+        pairs.append(p3m.pairCount())
+        p3m.setPairCounting(False)
     for _ in range(3):
         flush_l2()
         (p3m.force() if p3m else pm.pmMethodStep())
         stage = pm.stageTimes()
         pair_ms.append(stage["pair"])
-        if p3m:
-            pairs.append(p3m.pairCount())
     peaks, peak_src = load_peaks()
     fp32_peak = P.methods.fp32_peak_tflops()
     roofline = None
@@ -296,6 +305,9 @@ def run_ours(args):
     if p3m:
         p3m.close()
     pm.close()
+    closure = None
+    if world == 1 and not args.no_closure and args.workload == "disk_p3m":
+        closure = closure_compare(args, flush_l2)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -304,10 +316,93 @@ def run_ours(args):
                 "config": {**config_of(w), "l2": "256 MB L2 flush before every timed step"},
                 "e2e": e2e, "roofline": roofline, "roofline_pm": roofline_pm,
                 "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
-                "impl": "ours"}
+                "closure": closure, "impl": "ours"}
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def closure_compare(args, flush_l2=None, steps=None):
+    """Plain P3M vs the learned closure on the 1,048,576-particle disk (128^3, TSC, S2, cutoff
+    3 mesh cells; closure pair cutoff 1.5 cells): training pairs from the plain P3M at t = 0 and
+    after 50 steps (2 x 1,048,576 rows), GPU training, then device-timed steps of both modes and
+    the median relative force error of both against an FP64 direct sum on 8,192 particles."""
+    import numpy as np
+
+    import particlesimulation_gb300 as P
+    from oracle import oracle as O
+    from particlesimulation_gb300 import workloads as W
+
+    steps = steps or args.steps
+    w = W.disk_p3m_1m()
+    pm = P.PMMethod(w.state, w.mass, w.box, None, w.H, w.DT, w.G,
+                    P.InterpolationScheme(w.interpolation), P.FiniteDiffScheme(w.finite_diff),
+                    P.GreensFunction(w.greens), w.diameter, w.grid)
+    q = w.p3m
+    cl = P.LearnedClosure(pm, q["comp_box"], q["cutoff"], q["diameter"], q["softening"],
+                          P.CloudShape(q["cloud_shape"]), 0.5 * q["cutoff"], capacity=2 * w.n,
+                          seed=args.seed)
+    t0 = time.perf_counter()
+    cl.collect()
+    pm.run(0)
+    pm.advance(50)
+    rows = cl.collect()
+    t1 = time.perf_counter()
+    loss = cl.train(epochs=args.closure_epochs, batch=4096, lr=2e-3)
+    t2 = time.perf_counter()
+    flush_l2 = flush_l2 or (lambda: None)
+
+    def timed(mode):
+        cl.setMode(mode)
+        for _ in range(args.warmup):
+            pm.advance(1)
+        tot = 0.0
+        for _ in range(steps):
+            flush_l2()
+            esc, _, ms = pm.advance(1)
+            if esc:
+                raise RuntimeError("a particle left the box")
+            tot += ms
+        return tot / steps
+
+    ms_plain = timed(cl.FULL)
+    ms_learned = timed(cl.LEARNED)
+    judge = cl.judge(stride=16)
+    # forces at the same positions in both modes, original units
+    cl.setMode(cl.FULL)
+    cl.force()
+    x, _, a_plain = pm.getParticles(units="original")
+    cl.setMode(cl.LEARNED)
+    cl.force()
+    _, _, a_learned = pm.getParticles(units="original")
+    cl.setMode(cl.REDUCED_ONLY)
+    cl.force()
+    _, _, a_reduced = pm.getParticles(units="original")
+    rng = np.random.default_rng(12345)
+    idx = np.sort(rng.choice(w.n, 8192, replace=False)).astype(np.int32)
+    t3 = time.perf_counter()
+    a_pp = O.port_pp_accel(x.astype(np.float64), w.mass.astype(np.float64), w.G, idx=idx)
+    t4 = time.perf_counter()
+
+    def med(a):
+        d = np.linalg.norm(a[idx].astype(np.float64) - a_pp, axis=1)
+        return float(np.median(d / np.linalg.norm(a_pp, axis=1)))
+
+    out = {"workload": f"{w.name}: {w.n:,} particles, {w.grid[0]}^3, TSC, S2, cutoff 3 mesh cells; "
+                       "closure pair cutoff 1.5 cells",
+           "plain_p3m": {"value": w.n / (ms_plain * 1e-3), "ms_per_step": ms_plain,
+                         "median_rel_force_err_vs_fp64_direct": med(a_plain)},
+           "learned_closure": {"value": w.n / (ms_learned * 1e-3), "ms_per_step": ms_learned,
+                               "median_rel_force_err_vs_fp64_direct": med(a_learned),
+                               "median_rel_err_vs_plain_p3m": judge},
+           "reduced_cutoff_alone": {"median_rel_force_err_vs_fp64_direct": med(a_reduced)},
+           "speedup": ms_plain / ms_learned,
+           "training": {"rows": rows, "epochs": args.closure_epochs, "final_mse": loss,
+                        "collect_s": t1 - t0, "train_s": t2 - t1},
+           "direct_sum": {"targets": 8192, "sources": w.n, "seconds": t4 - t3, "precision": "fp64"}}
+    cl.close()
+    pm.close()
+    return out
 
 
 def run_reference(args):

@@ -187,6 +187,57 @@ int pmgb_p3m_get_sr_table(pmgb_p3m* p3m, float* table500, float* delta_sq);
  * (each unordered pair counts twice).  No reference counterpart: it sizes the pair pass's
  * FLOP count (20 FLOP per unordered pair). */
 int pmgb_p3m_pair_count(pmgb_p3m* p3m, unsigned long long* ordered_pairs);
+/* Turns the in-range pair counter of force evaluations on or off (off by default; counting
+ * costs a few percent of the pair pass). */
+int pmgb_p3m_set_pair_counting(pmgb_p3m* p3m, int enable);
+
+/* ---------------------------------------------------------------- learned closure ---- */
+/* No counterpart in the reference.  A plain P3M pair pass at cutoff re is replaced by one at a
+ * reduced cutoff re' plus an MLP that predicts the missing short-range force of the pairs at
+ * re' <= r < re from the 4x4x4 patch of cell masses of the reduced chaining mesh around each
+ * particle and its in-cell offset (67 inputs, 3 hidden GELU layers of 64, BF16 weights, FP32
+ * accumulation, tensor-core kernels).  It is trained on the GPU on residuals the plain P3M
+ * itself produces; the plain P3M judges it and is the fallback.  Modes: */
+#define PMGB_CLOSURE_FULL 0         /* plain P3M at the full cutoff */
+#define PMGB_CLOSURE_LEARNED 1      /* reduced-cutoff pair pass + learned residual */
+#define PMGB_CLOSURE_REDUCED_ONLY 2 /* reduced-cutoff pair pass alone (what the MLP adds to) */
+
+typedef struct pmgb_closure pmgb_closure;
+
+/* Creates the full- and reduced-cutoff pair passes over `pm` (which must have no P3M handle;
+ * destroy the closure before the PM handle), `capacity` training rows, parameters initialised
+ * from `seed`.  Starts in PMGB_CLOSURE_FULL. */
+int pmgb_closure_create(pmgb_pm* pm, const pmgb_p3m_config* full_cfg, float reduced_cutoff,
+                        int capacity, unsigned long long seed, pmgb_closure** out);
+int pmgb_closure_destroy(pmgb_closure* c);
+int pmgb_closure_set_mode(pmgb_closure* c, int mode);
+int pmgb_closure_get_mode(pmgb_closure* c, int* mode);
+/* Adds (features, residual) rows for every `stride`-th particle at the current positions:
+ * residual = full-cutoff minus reduced-cutoff P3M acceleration.  *total = rows collected. */
+int pmgb_closure_collect(pmgb_closure* c, int stride, int* total);
+/* Adam on the collected rows (mean squared error, cosine learning-rate decay). */
+int pmgb_closure_train(pmgb_closure* c, int epochs, int batch, float lr, float* final_loss);
+int pmgb_closure_param_count(void);
+int pmgb_closure_get_params(pmgb_closure* c, float* params, int count);
+int pmgb_closure_set_params(pmgb_closure* c, const float* params, int count);
+/* Median relative difference between the learned and the full-cutoff P3M accelerations over
+ * every `stride`-th particle at the current positions. */
+int pmgb_closure_judge(pmgb_closure* c, int stride, float* median_rel_err);
+/* n_steps run-loop iterations in the current mode; in PMGB_CLOSURE_LEARNED the judge runs every
+ * judge_interval steps and a median error above `bound` switches the rest of the run to plain
+ * P3M (*fallback_step = that step, else -1). */
+int pmgb_closure_run(pmgb_closure* c, int n_steps, float bound, int judge_interval,
+                     int judge_stride, int* steps_done, int* fallback_step, float* device_ms);
+/* Test support: the 67 inputs of every particle (original order) and its patch mass; the
+ * output scale c and the reduced mesh dimensions. */
+int pmgb_closure_features(pmgb_closure* c, float* x, float* spatch);
+int pmgb_closure_scales(pmgb_closure* c, float* out_scale, int* dims3);
+/* Test support: the MLP kernels on host data.  params: pmgb_closure_param_count() floats
+ * (W1 64x80, b1, W2 64x64, b2, W3 64x64, b3, W4 8x64, b4 8; padding zero).  x: n x 67,
+ * y: n x 3, t: n x 3 targets; gradients of the mean over rows of |y - t|^2. */
+int pmgb_mlp_eval(const float* params, int n, const float* x, float* y);
+int pmgb_mlp_gradients(const float* params, int n, const float* x, const float* t, float* grad,
+                       float* loss);
 
 /* ---------------------------------------------------------------- misc -------------- */
 /* FP32 FMA throughput of the current device in TFLOP/s, measured by a timed FMA kernel (the

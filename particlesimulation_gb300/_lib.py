@@ -21,6 +21,11 @@ EXPORTS = [
     "pmgb_pm_stage_times", "pmgb_pm_size", "pmgb_p3m_create", "pmgb_p3m_destroy",
     "pmgb_p3m_force", "pmgb_p3m_run", "pmgb_p3m_get_cell_lists", "pmgb_p3m_get_sr_table",
     "pmgb_p3m_pair_count", "pmgb_fp32_peak_probe", "pmgb_kernel_launches",
+    "pmgb_p3m_set_pair_counting",
+    "pmgb_closure_create", "pmgb_closure_destroy", "pmgb_closure_set_mode", "pmgb_closure_get_mode",
+    "pmgb_closure_collect", "pmgb_closure_train", "pmgb_closure_param_count",
+    "pmgb_closure_get_params", "pmgb_closure_set_params", "pmgb_closure_judge", "pmgb_closure_run",
+    "pmgb_closure_features", "pmgb_closure_scales", "pmgb_mlp_eval", "pmgb_mlp_gradients",
     "pmgb_last_error", "pmgb_version",
 ]
 
@@ -85,6 +90,22 @@ def lib() -> C.CDLL:
         L.pmgb_p3m_pair_count.argtypes = [vp, C.POINTER(C.c_ulonglong)]
         L.pmgb_fp32_peak_probe.argtypes = [fp]
         L.pmgb_kernel_launches.argtypes = [C.POINTER(C.c_longlong)]
+        L.pmgb_p3m_set_pair_counting.argtypes = [vp, C.c_int]
+        L.pmgb_closure_create.argtypes = [vp, C.POINTER(P3MConfigC), C.c_float, C.c_int,
+                                          C.c_ulonglong, C.POINTER(vp)]
+        L.pmgb_closure_destroy.argtypes = [vp]
+        L.pmgb_closure_set_mode.argtypes = [vp, C.c_int]
+        L.pmgb_closure_get_mode.argtypes = [vp, ip]
+        L.pmgb_closure_collect.argtypes = [vp, C.c_int, ip]
+        L.pmgb_closure_train.argtypes = [vp, C.c_int, C.c_int, C.c_float, fp]
+        L.pmgb_closure_get_params.argtypes = [vp, fp, C.c_int]
+        L.pmgb_closure_set_params.argtypes = [vp, fp, C.c_int]
+        L.pmgb_closure_judge.argtypes = [vp, C.c_int, fp]
+        L.pmgb_closure_run.argtypes = [vp, C.c_int, C.c_float, C.c_int, C.c_int, ip, ip, fp]
+        L.pmgb_closure_features.argtypes = [vp, fp, fp]
+        L.pmgb_closure_scales.argtypes = [vp, fp, ip]
+        L.pmgb_mlp_eval.argtypes = [fp, C.c_int, fp, fp]
+        L.pmgb_mlp_gradients.argtypes = [fp, C.c_int, fp, fp, fp, fp]
         L.pmgb_last_error.restype = C.c_char_p
         L.pmgb_version.restype = C.c_char_p
         _lib = L

@@ -20,43 +20,9 @@
 #include <string>
 #include <vector>
 
-#include "common.cuh"
+#include "handles.cuh"
 
 namespace pmgb {
-
-// kernels (other translation units)
-int radix_hist_blocks(int n);
-int radix_sort_pairs(u64** keys, u32** vals, u64** keys_alt, u32** vals_alt, u32* hist, int n,
-                     int nbits, cudaStream_t st);
-int launch_chain_keys(const float4* pm, const float4* vi, int n, ChainDims c, int ysort,
-                      const int* stop, u64* keys, u32* vals, cudaStream_t st);
-int launch_fix_ties(const u64* keys, u32* vals, const float4* vi, int n, const int* stop,
-                    cudaStream_t st);
-int launch_brick_keys(const float4* pm, int n, MeshDims m, int bshift, const int* stop, u64* keys,
-                      u32* vals, cudaStream_t st);
-int launch_gather(const u64* keys, const u32* vals, int n, const float4* pm_in,
-                  const float4* vi_in, float4* pm_out, float4* vi_out, int* cell_start,
-                  int ncells_total, const int* stop, cudaStream_t st);
-int launch_deposit(int is, const float4* pm, int n, MeshDims m, float scale, u64* rho,
-                   const int* stop, cudaStream_t st);
-int fft_configure(const MeshDims& m);
-int launch_poisson(u64* rho, float2* spec, float* phi, const float* ghat, const float2* tw,
-                   int nmax, MeshDims m, float fx_inv, const int* stop, cudaStream_t st);
-int launch_green(float* ghat, MeshDims m, int gf, int is, int fds, double a, cudaStream_t st);
-int launch_interp(bool kdk, float4* pm, float4* vi, float4* acc, int n, const float* phi,
-                  const StepParams& sp, float kick, int drift, int* stop, cudaStream_t st);
-int launch_kick_drift(float4* pm, float4* vi, const float4* acc, int n, const StepParams& sp,
-                      float kick, int drift, int* stop, cudaStream_t st);
-int launch_unpack(const float4* pm, const float4* vi, const float4* acc, int n, float H, float DT,
-                  int orig, float* pos, float* vel, float* aout, cudaStream_t st);
-int launch_pack(const float* pos, const float* vel, const float* mass_code, int n, float H,
-                float DT, int orig, float4* pm, float4* vi, cudaStream_t st);
-int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const int* cell_start,
-                int Mx, int My, int Mz, u32* item_cnt, u32* item_off, u32* nitems, int2* items,
-                u32* counter, const PairParams& pp, const float* table, const StepParams& sp,
-                float kick, int drift, int kdk, float4* pm_out, float4* vi_out, float4* acc_out,
-                unsigned long long* npairs, int* stop, int num_sms, cudaEvent_t ev_pair,
-                cudaStream_t st);
 
 static thread_local std::string g_last_error;
 void set_error(const std::string& msg) { g_last_error = msg; }
@@ -73,52 +39,6 @@ static bool pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
 }  // namespace pmgb
 
 using namespace pmgb;
-
-struct pmgb_p3m;
-
-struct pmgb_pm {
-  pmgb_pm_config cfg{};
-  int n = 0;
-  MeshDims m{};
-  StepParams sp{};
-  cudaStream_t st = nullptr;
-  int num_sms = 0;
-  float4* pm[2] = {nullptr, nullptr};
-  float4* vi[2] = {nullptr, nullptr};
-  float4* acc = nullptr;
-  float4* acc_pm = nullptr;
-  int cur = 0;
-  u64 *keys = nullptr, *keys_alt = nullptr;
-  u32 *vals = nullptr, *vals_alt = nullptr, *hist = nullptr;
-  u64* rho = nullptr;
-  float2* spec = nullptr;
-  float* phi = nullptr;
-  float* ghat = nullptr;
-  float2* tw = nullptr;
-  int nmax = 0;
-  int* flags = nullptr;  // device: [0] stop, [1] escape iteration
-  pmgb_p3m* p3m = nullptr;
-  int since_sort = 1 << 30;
-  cudaEvent_t ev[6] = {};
-  float stage_ms[5] = {0, 0, 0, 0, 0};
-  float* stage = nullptr;      // 9 n floats: positions, velocities, accelerations (original order)
-  float* mass_code = nullptr;  // n floats, code-unit masses in original order
-};
-
-struct pmgb_p3m {
-  pmgb_pm* pm = nullptr;
-  pmgb_p3m_config cfg{};
-  ChainDims cd{};
-  int ncells = 0;
-  int* cell_start = nullptr;  // ncells + 2
-  u32 *item_cnt = nullptr, *item_off = nullptr, *nitems = nullptr, *counter = nullptr;
-  int2* items = nullptr;
-  float* table = nullptr;
-  float table_h[500];
-  float delta2 = 0;
-  PairParams pp{};
-  unsigned long long* npairs = nullptr;
-};
 
 namespace {
 
@@ -256,11 +176,15 @@ int force(pmgb_pm* h, int kdk, float kick, int drift, int tag, bool timed) {
   }
   rc = launch_interp(false, h->pm[h->cur], h->vi[h->cur], h->acc_pm, n, h->phi, sp, kick, drift, stop, h->st);
   if (rc) return rc;
+  if (h->closure) {
+    rc = closure_apply(h);
+    if (rc) return rc;
+  }
   // ev[4] is recorded just before the pair kernel (after its work-item setup)
   rc = launch_pair(h->pm[h->cur], h->vi[h->cur], h->acc_pm, q->cell_start, q->cd.Mx, q->cd.My, q->cd.Mz,
                    q->item_cnt, q->item_off, q->nitems, q->items, q->counter, q->pp, q->table, sp,
                    kick, drift, kdk, h->pm[1 - h->cur], h->vi[1 - h->cur], h->acc,
-                   timed ? q->npairs : nullptr, stop,
+                   q->count_pairs ? q->npairs : nullptr, stop,
                    h->num_sms, timed ? h->ev[4] : nullptr, h->st);
   if (rc) return rc;
   if (kdk) {
@@ -595,7 +519,16 @@ int pmgb_pm_size(pmgb_pm* h, int* n, int* grid3) {
 int pmgb_p3m_create(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out) {
   if (!pm || !cfg || !out) return set_error("null argument"), PMGB_EINVAL;
   *out = nullptr;
-  if (pm->p3m) return set_error("this PM handle already has a P3M handle"), PMGB_EINVAL;
+  if (pm->p3m || pm->closure) return set_error("this PM handle already has a P3M handle"), PMGB_EINVAL;
+  return pmgb::p3m_create_internal(pm, cfg, out, true);
+}
+
+}  // extern "C"
+
+namespace pmgb {
+// P3M handle over `pm`; attach = make it the PM handle's pair pass now (a closure keeps two
+// detached handles and switches between them).
+int p3m_create_internal(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out, bool attach) {
   if (!(cfg->cutoff > 0)) return set_error("cutoff radius must be positive"), PMGB_EINVAL;
   if (cfg->cloud_shape != PMGB_S1 && cfg->cloud_shape != PMGB_S2) return set_error("not implemented"), PMGB_EINVAL;
   pmgb_p3m* q = new pmgb_p3m();
@@ -663,10 +596,13 @@ int pmgb_p3m_create(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out) {
     pmgb_p3m_destroy(q);
     return set_error("P3M table upload failed"), PMGB_ECUDA;
   }
-  pm->p3m = q;
+  if (attach) pm->p3m = q;
   *out = q;
   return PMGB_OK;
 }
+}  // namespace pmgb
+
+extern "C" {
 
 int pmgb_p3m_destroy(pmgb_p3m* q) {
   if (!q) return PMGB_OK;
@@ -713,6 +649,12 @@ int pmgb_p3m_get_cell_lists(pmgb_p3m* q, int* order, int* counts, int* dims3) {
     const int inside = cs[q->ncells];
     for (int k = 0; k < inside; ++k) std::memcpy(&order[k], &hv[k].w, 4);
   }
+  return PMGB_OK;
+}
+
+int pmgb_p3m_set_pair_counting(pmgb_p3m* q, int enable) {
+  if (!q) return set_error("null handle"), PMGB_EINVAL;
+  q->count_pairs = enable ? 1 : 0;
   return PMGB_OK;
 }
 

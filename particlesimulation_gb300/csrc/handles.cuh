@@ -1,0 +1,99 @@
+// handles.cuh - the handle structures behind the C ABI and the launchers shared between
+// translation units.
+#pragma once
+#include "common.cuh"
+
+namespace pmgb {
+
+int radix_hist_blocks(int n);
+int radix_sort_pairs(u64** keys, u32** vals, u64** keys_alt, u32** vals_alt, u32* hist, int n,
+                     int nbits, cudaStream_t st);
+int exclusive_scan(const u32* in, u32* out, int n, u32* total, cudaStream_t st);
+int launch_chain_keys(const float4* pm, const float4* vi, int n, ChainDims c, int ysort,
+                      const int* stop, u64* keys, u32* vals, cudaStream_t st);
+int launch_fix_ties(const u64* keys, u32* vals, const float4* vi, int n, const int* stop,
+                    cudaStream_t st);
+int launch_brick_keys(const float4* pm, int n, MeshDims m, int bshift, const int* stop, u64* keys,
+                      u32* vals, cudaStream_t st);
+int launch_gather(const u64* keys, const u32* vals, int n, const float4* pm_in,
+                  const float4* vi_in, float4* pm_out, float4* vi_out, int* cell_start,
+                  int ncells_total, const int* stop, cudaStream_t st);
+int launch_deposit(int is, const float4* pm, int n, MeshDims m, float scale, u64* rho,
+                   const int* stop, cudaStream_t st);
+int fft_configure(const MeshDims& m);
+int launch_poisson(u64* rho, float2* spec, float* phi, const float* ghat, const float2* tw,
+                   int nmax, MeshDims m, float fx_inv, const int* stop, cudaStream_t st);
+int launch_green(float* ghat, MeshDims m, int gf, int is, int fds, double a, cudaStream_t st);
+int launch_interp(bool kdk, float4* pm, float4* vi, float4* acc, int n, const float* phi,
+                  const StepParams& sp, float kick, int drift, int* stop, cudaStream_t st);
+int launch_kick_drift(float4* pm, float4* vi, const float4* acc, int n, const StepParams& sp,
+                      float kick, int drift, int* stop, cudaStream_t st);
+int launch_unpack(const float4* pm, const float4* vi, const float4* acc, int n, float H, float DT,
+                  int orig, float* pos, float* vel, float* aout, cudaStream_t st);
+int launch_pack(const float* pos, const float* vel, const float* mass_code, int n, float H,
+                float DT, int orig, float4* pm, float4* vi, cudaStream_t st);
+int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const int* cell_start,
+                int Mx, int My, int Mz, u32* item_cnt, u32* item_off, u32* nitems, int2* items,
+                u32* counter, const PairParams& pp, const float* table, const StepParams& sp,
+                float kick, int drift, int kdk, float4* pm_out, float4* vi_out, float4* acc_out,
+                unsigned long long* npairs, int* stop, int num_sms, cudaEvent_t ev_pair,
+                cudaStream_t st);
+
+}  // namespace pmgb
+
+struct pmgb_p3m;
+struct pmgb_closure;
+
+struct pmgb_pm {
+  pmgb_pm_config cfg{};
+  int n = 0;
+  pmgb::MeshDims m{};
+  pmgb::StepParams sp{};
+  cudaStream_t st = nullptr;
+  int num_sms = 0;
+  float4* pm[2] = {nullptr, nullptr};
+  float4* vi[2] = {nullptr, nullptr};
+  float4* acc = nullptr;
+  float4* acc_pm = nullptr;
+  int cur = 0;
+  pmgb::u64 *keys = nullptr, *keys_alt = nullptr;
+  pmgb::u32 *vals = nullptr, *vals_alt = nullptr, *hist = nullptr;
+  pmgb::u64* rho = nullptr;
+  float2* spec = nullptr;
+  float* phi = nullptr;
+  float* ghat = nullptr;
+  float2* tw = nullptr;
+  int nmax = 0;
+  int* flags = nullptr;  // device: [0] stop, [1] escape iteration
+  pmgb_p3m* p3m = nullptr;
+  pmgb_closure* closure = nullptr;  // learned short-range closure applied after interpolation
+  int since_sort = 1 << 30;
+  cudaEvent_t ev[6] = {};
+  float stage_ms[5] = {0, 0, 0, 0, 0};
+  float* stage = nullptr;      // 9 n floats: positions, velocities, accelerations (original order)
+  float* mass_code = nullptr;  // n floats, code-unit masses in original order
+};
+
+struct pmgb_p3m {
+  pmgb_pm* pm = nullptr;
+  pmgb_p3m_config cfg{};
+  pmgb::ChainDims cd{};
+  int ncells = 0;
+  int* cell_start = nullptr;  // ncells + 2
+  pmgb::u32 *item_cnt = nullptr, *item_off = nullptr, *nitems = nullptr, *counter = nullptr;
+  int2* items = nullptr;
+  float* table = nullptr;
+  float table_h[500];
+  float delta2 = 0;
+  pmgb::PairParams pp{};
+  unsigned long long* npairs = nullptr;
+  int count_pairs = 0;  // count in-range pairs during force evaluations (pmgb_p3m_set_pair_counting)
+};
+
+namespace pmgb {
+// Adds the closure's predicted residual short-range acceleration to h->acc_pm (sorted order of
+// h->pm[h->cur]); defined in closure.cu.
+int closure_apply(pmgb_pm* h);
+// P3M handle over pm; attach = make it pm's pair pass (api.cu).
+int p3m_create_internal(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out, bool attach);
+}  // namespace pmgb

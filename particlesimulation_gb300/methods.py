@@ -267,6 +267,9 @@ class P3MMethod:
     def advance(self, nSteps: int):
         return self.pm.advance(nSteps)
 
+    def setPairCounting(self, enable: bool):
+        check(lib().pmgb_p3m_set_pair_counting(self._h, int(bool(enable))))
+
     def pairCount(self) -> int:
         """Ordered pairs within the cutoff in the last force evaluation."""
         c = C.c_ulonglong(0)
@@ -278,3 +281,121 @@ class P3MMethod:
         d2 = C.c_float(0)
         check(lib().pmgb_p3m_get_sr_table(self._h, _fp(t), C.byref(d2)))
         return t, d2.value
+
+
+class LearnedClosure:
+    """Learned short-range closure over a PM handle (no counterpart in the reference): the
+    full-cutoff pair pass of P3M (plain P3M, the judge and fallback) and a reduced-cutoff pair
+    pass whose missing residual an MLP predicts (include/pmgb.h, pmgb_closure_*)."""
+
+    FULL, LEARNED, REDUCED_ONLY = 0, 1, 2
+
+    def __init__(self, pm: PMMethod, compBoxSize, cutoffRadius, particleDiameter,
+                 softeningLength, cloudShape: CloudShape, reducedCutoff, capacity=0, seed=0,
+                 useSRForceTable: bool = True, enableYSorting: bool = True):
+        cfg = _lib.P3MConfigC()
+        cfg.comp_box[:] = [float(b) for b in compBoxSize]
+        cfg.cutoff = float(cutoffRadius)
+        cfg.particle_diameter = float(particleDiameter)
+        cfg.softening = float(softeningLength)
+        cfg.cloud_shape = int(cloudShape)
+        cfg.use_table = int(bool(useSRForceTable))
+        cfg.y_sorting = int(bool(enableYSorting))
+        h = C.c_void_p()
+        check(lib().pmgb_closure_create(pm._h, C.byref(cfg), C.c_float(reducedCutoff), int(capacity),
+                                        C.c_ulonglong(seed), C.byref(h)))
+        self._h = h
+        self.pm = pm
+        pm._p3m = self
+
+    def close(self):
+        if getattr(self, "_h", None):
+            check(lib().pmgb_closure_destroy(self._h))
+            self._h = None
+            self.pm._p3m = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def setMode(self, mode: int):
+        check(lib().pmgb_closure_set_mode(self._h, int(mode)))
+
+    def mode(self) -> int:
+        m = C.c_int(0)
+        check(lib().pmgb_closure_get_mode(self._h, C.byref(m)))
+        return m.value
+
+    def collect(self, stride: int = 1) -> int:
+        total = C.c_int(0)
+        check(lib().pmgb_closure_collect(self._h, int(stride), C.byref(total)))
+        return total.value
+
+    def train(self, epochs: int, batch: int = 4096, lr: float = 2e-3) -> float:
+        loss = C.c_float(0)
+        check(lib().pmgb_closure_train(self._h, int(epochs), int(batch), C.c_float(lr), C.byref(loss)))
+        return float(loss.value)
+
+    def params(self):
+        n = lib().pmgb_closure_param_count()
+        p = np.zeros(n, np.float32)
+        check(lib().pmgb_closure_get_params(self._h, _fp(p), n))
+        return p
+
+    def setParams(self, p):
+        p = _f32(p).reshape(-1)
+        check(lib().pmgb_closure_set_params(self._h, _fp(p), len(p)))
+
+    def judge(self, stride: int = 1) -> float:
+        e = C.c_float(0)
+        check(lib().pmgb_closure_judge(self._h, int(stride), C.byref(e)))
+        return float(e.value)
+
+    def run(self, nSteps: int, bound: float, judgeInterval: int, judgeStride: int = 1):
+        """(escaped, steps_done, fallback_step or -1, device_ms)"""
+        done, fb, ms = C.c_int(0), C.c_int(-1), C.c_float(0)
+        rc = check(lib().pmgb_closure_run(self._h, int(nSteps), C.c_float(bound), int(judgeInterval),
+                                          int(judgeStride), C.byref(done), C.byref(fb), C.byref(ms)))
+        return rc == _lib.PMGB_EESCAPED, done.value, fb.value, ms.value
+
+    def force(self):
+        check(lib().pmgb_pm_method_step(self.pm._h))
+
+    def features(self):
+        n = self.pm.N
+        x = np.zeros((n, 67), np.float32)
+        s = np.zeros(n, np.float32)
+        check(lib().pmgb_closure_features(self._h, _fp(x), _fp(s)))
+        return x, s
+
+    def scales(self):
+        c = C.c_float(0)
+        d = (C.c_int * 3)()
+        check(lib().pmgb_closure_scales(self._h, C.byref(c), d))
+        return float(c.value), (d[0], d[1], d[2])
+
+
+def mlp_param_count() -> int:
+    return int(lib().pmgb_closure_param_count())
+
+
+def mlp_eval(params, x):
+    """The closure MLP (our tensor-core kernels) on host inputs x (n, 67) -> (n, 3)."""
+    p = _f32(params).reshape(-1)
+    x = _f32(x).reshape(-1, 67)
+    y = np.zeros((len(x), 3), np.float32)
+    check(lib().pmgb_mlp_eval(_fp(p), len(x), _fp(x), _fp(y)))
+    return y
+
+
+def mlp_gradients(params, x, t):
+    """Gradient of mean_rows |MLP(x) - t|^2 w.r.t. the parameters, by our training kernels."""
+    p = _f32(params).reshape(-1)
+    x = _f32(x).reshape(-1, 67)
+    t = _f32(t).reshape(-1, 3)
+    g = np.zeros_like(p)
+    loss = C.c_float(0)
+    check(lib().pmgb_mlp_gradients(_fp(p), len(x), _fp(x), _fp(t), _fp(g), C.byref(loss)))
+    return g, float(loss.value)
