@@ -239,6 +239,21 @@ int pmgb_mlp_eval(const float* params, int n, const float* x, float* y);
 int pmgb_mlp_gradients(const float* params, int n, const float* x, const float* t, float* grad,
                        float* loss);
 
+/* Chaining-mesh cell lists built without allocating any device memory.  No counterpart in the
+ * reference: it is for callers that cannot allocate device memory where they need the lists
+ * (hosts that hand the library buffers from their own fixed pool, or step loops that must not
+ * call cudaMalloc).  Same lists as pmgb_p3m_get_cell_lists: d_pos = n xyz triplets in code
+ * units (device memory), d_order = n ints, d_counts = Mx*My*Mz ints (device memory), dims3 =
+ * (Mx, My, Mz) on the host; cfg supplies comp_box, cutoff and y_sorting.  Runs on `stream`
+ * (a cudaStream_t, NULL = default stream) without synchronising.  Limits: n <= 262,144 and
+ * Mx*My*Mz <= 262,142; larger inputs return PMGB_EINVAL.  Its scratch (about 6.5 MB) is a
+ * fixed device array held on every GPU that loads the library; the first call on a device
+ * looks its address up (call it once before any stream capture); calls that overlap on the
+ * GPU share the scratch and race. */
+int pmgb_chaining_mesh_fill_noalloc(const float* d_pos, int n, const pmgb_p3m_config* cfg,
+                                    float H, int* d_order, int* d_counts, int* dims3,
+                                    void* stream);
+
 /* ---------------------------------------------------------------- misc -------------- */
 /* FP32 FMA throughput of the current device in TFLOP/s, measured by a timed FMA kernel (the
  * roofline denominator of the FP32-bound pair pass).  No reference counterpart. */
