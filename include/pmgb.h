@@ -191,6 +191,31 @@ int pmgb_p3m_pair_count(pmgb_p3m* p3m, unsigned long long* ordered_pairs);
  * costs a few percent of the pair pass). */
 int pmgb_p3m_set_pair_counting(pmgb_p3m* p3m, int enable);
 
+/* ---------------------------------------------------------------- ensemble ----------- */
+/* No counterpart in the reference (one system per process there).  n_systems independent PM
+ * systems, each exactly a pmgb_pm (cfgs[s], counts[s] particles, states[s] = positions then
+ * velocities, masses[s]), advanced together: every stage of a step is one launch over all
+ * systems (persistent kernels over a table of systems and work items), each step one CUDA
+ * graph.  All systems share the interpolation and difference schemes; meshes, particle
+ * counts, boxes, Green's functions and external fields may differ.  Tile shapes are picked at
+ * creation by timing candidates (they do not change results: each system is bit-identical to
+ * the same system run by a pmgb_pm handle). */
+typedef struct pmgb_ensemble pmgb_ensemble;
+int pmgb_ensemble_create(int n_systems, const pmgb_pm_config* cfgs, const int* counts,
+                         const float* const* states, const float* const* masses,
+                         pmgb_ensemble** out);
+int pmgb_ensemble_destroy(pmgb_ensemble* e);
+/* PMMethod::run for every system (escaped[s] = 1 where system s stopped on an escape). */
+int pmgb_ensemble_run(pmgb_ensemble* e, int sim_length, int* escaped, float* device_ms);
+/* n_steps more loop iterations of every system, continuing from run(). */
+int pmgb_ensemble_advance(pmgb_ensemble* e, int n_steps, float* device_ms);
+int pmgb_ensemble_get_particles(pmgb_ensemble* e, int system, float* pos, float* vel, float* acc,
+                                int units);
+/* Autotuner choices: particles per deposit thread, x-pass rows per CTA (0: half, 1: default,
+ * 2: double the default), and the six candidate timings in ms. */
+int pmgb_ensemble_tuning(pmgb_ensemble* e, int* deposit_ppt, int* x_rows_mult, float* timings6);
+int pmgb_ensemble_size(pmgb_ensemble* e, int* n_systems, long long* total_particles);
+
 /* ---------------------------------------------------------------- learned closure ---- */
 /* No counterpart in the reference.  A plain P3M pair pass at cutoff re is replaced by one at a
  * reduced cutoff re' plus an MLP that predicts the missing short-range force of the pairs at

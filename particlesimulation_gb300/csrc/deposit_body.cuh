@@ -1,0 +1,151 @@
+// deposit_body.cuh - the deposit of one chunk of particles by one CTA (shared by the
+// single-system and the ensemble kernels, so both compute bit-identical densities).
+// See deposit.cu for the method.
+#pragma once
+#include "common.cuh"
+
+namespace pmgb {
+
+constexpr int DEP_THREADS = 256;
+constexpr int DEP_PPT = 2;                               // particles per thread
+constexpr int DEP_CHUNK = DEP_THREADS * DEP_PPT;
+constexpr int DEP_TILE = 4096;                           // u64 cells in the shared tile (32 KB)
+
+template <int IS>
+struct Stencil;
+template <>
+struct Stencil<0> { static constexpr int lo = 0, hi = 0; };
+template <>
+struct Stencil<1> { static constexpr int lo = 0, hi = 1; };
+template <>
+struct Stencil<2> { static constexpr int lo = 1, hi = 1; };
+
+__device__ __forceinline__ long long to_fixed(float w, float scale) {
+  return __float2ll_rn(__fmul_rn(w, scale));
+}
+
+// Calls emit(ix, iy, iz, fixed_value) for every stencil cell of particle p.
+template <int IS, typename F>
+__device__ __forceinline__ void stencil(const float4 p, float scale, F&& emit) {
+  const float d = p.w;
+  if (IS == 0) {
+    int x = (int)roundf(p.x), y = (int)roundf(p.y), z = (int)roundf(p.z);
+    emit(x, y, z, to_fixed(d, scale));
+  } else if (IS == 1) {
+    int x = (int)p.x, y = (int)p.y, z = (int)p.z;
+    float dx = fsub(p.x, (float)x), dy = fsub(p.y, (float)y), dz = fsub(p.z, (float)z);
+    float tx = fsub(1.0f, dx), ty = fsub(1.0f, dy), tz = fsub(1.0f, dz);
+    emit(x, y, z, to_fixed(fmul(fmul(fmul(d, tx), ty), tz), scale));
+    emit(x + 1, y, z, to_fixed(fmul(fmul(fmul(d, dx), ty), tz), scale));
+    emit(x, y + 1, z, to_fixed(fmul(fmul(fmul(d, tx), dy), tz), scale));
+    emit(x, y, z + 1, to_fixed(fmul(fmul(fmul(d, tx), ty), dz), scale));
+    emit(x + 1, y + 1, z, to_fixed(fmul(fmul(fmul(d, dx), dy), tz), scale));
+    emit(x + 1, y, z + 1, to_fixed(fmul(fmul(fmul(d, dx), ty), dz), scale));
+    emit(x, y + 1, z + 1, to_fixed(fmul(fmul(fmul(d, tx), dy), dz), scale));
+    emit(x + 1, y + 1, z + 1, to_fixed(fmul(fmul(fmul(d, dx), dy), dz), scale));
+  } else {
+    int x = (int)p.x, y = (int)p.y, z = (int)p.z;
+    float dx = fsub(p.x, (float)x), dy = fsub(p.y, (float)y), dz = fsub(p.z, (float)z);
+    const float d8 = __fdiv_rn(d, 8.0f);
+#pragma unroll
+    for (int t1 = -1; t1 <= 1; ++t1) {
+      float T1 = fmul(d8, tsc_w(dx, t1));
+#pragma unroll
+      for (int t2 = -1; t2 <= 1; ++t2) {
+        float T2 = fmul(T1, tsc_w(dy, t2));
+#pragma unroll
+        for (int t3 = -1; t3 <= 1; ++t3) {
+          float T3 = fmul(T2, tsc_w(dz, t3));
+          emit(x + t1, y + t2, z + t3, to_fixed(T3, scale));
+        }
+      }
+    }
+  }
+}
+
+template <int IS>
+__device__ __forceinline__ void base_cell(const float4 p, int& x, int& y, int& z) {
+  if (IS == 0) {
+    x = (int)roundf(p.x);
+    y = (int)roundf(p.y);
+    z = (int)roundf(p.z);
+  } else {
+    x = (int)p.x;
+    y = (int)p.y;
+    z = (int)p.z;
+  }
+}
+
+__device__ __forceinline__ int block_min(int v, int* red) {
+  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+  const int w = threadIdx.x >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[w] = v;
+  __syncthreads();
+  v = red[0];
+  for (int i = 1; i < DEP_THREADS / 32; ++i) v = min(v, red[i]);
+  return v;
+}
+__device__ __forceinline__ int block_max(int v, int* red) { return -block_min(-v, red); }
+
+template <int IS, int PPT>
+__device__ __forceinline__ void deposit_block(const float4* __restrict__ pm, int base, int n,
+                                              const MeshDims& m, float scale, u64* __restrict__ rho,
+                                              u64* tile, int* red) {
+  float4 p[PPT];
+  bool valid[PPT];
+  int mnx = 1 << 30, mny = 1 << 30, mnz = 1 << 30, mxx = -(1 << 30), mxy = -(1 << 30), mxz = -(1 << 30);
+#pragma unroll
+  for (int k = 0; k < PPT; ++k) {
+    int i = base + k * DEP_THREADS + threadIdx.x;
+    valid[k] = i < n;
+    if (valid[k]) {
+      p[k] = pm[i];
+      int x, y, z;
+      base_cell<IS>(p[k], x, y, z);
+      mnx = min(mnx, x); mny = min(mny, y); mnz = min(mnz, z);
+      mxx = max(mxx, x); mxy = max(mxy, y); mxz = max(mxz, z);
+    }
+  }
+  mnx = block_min(mnx, red); mny = block_min(mny, red); mnz = block_min(mnz, red);
+  mxx = block_max(mxx, red); mxy = block_max(mxy, red); mxz = block_max(mxz, red);
+  const int ox = mnx - Stencil<IS>::lo, oy = mny - Stencil<IS>::lo, oz = mnz - Stencil<IS>::lo;
+  const int ex = mxx - mnx + Stencil<IS>::lo + Stencil<IS>::hi + 1;
+  const int ey = mxy - mny + Stencil<IS>::lo + Stencil<IS>::hi + 1;
+  const int ez = mxz - mnz + Stencil<IS>::lo + Stencil<IS>::hi + 1;
+  const long long vol = (long long)ex * ey * ez;
+  const bool use_tile = vol <= DEP_TILE && ex <= m.nx && ey <= m.ny && ez <= m.nz;
+  const size_t sxy = (size_t)m.nx * m.ny;
+
+  if (use_tile) {
+    for (int c = threadIdx.x; c < (int)vol; c += DEP_THREADS) tile[c] = 0ull;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+      if (!valid[k]) continue;
+      stencil<IS>(p[k], scale, [&](int x, int y, int z, long long v) {
+        int c = (x - ox) + ex * ((y - oy) + ey * (z - oz));
+        atomicAdd(&tile[c], (u64)v);
+      });
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < (int)vol; c += DEP_THREADS) {
+      u64 v = tile[c];
+      if (v == 0ull) continue;
+      int x = ox + c % ex, y = oy + (c / ex) % ey, z = oz + c / (ex * ey);
+      fx_add_global(&rho[(size_t)wrapi(z, m.nz) * sxy + (size_t)wrapi(y, m.ny) * m.nx + wrapi(x, m.nx)],
+                    (long long)v);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+      if (!valid[k]) continue;
+      stencil<IS>(p[k], scale, [&](int x, int y, int z, long long v) {
+        fx_add_global(&rho[(size_t)wrapi(z, m.nz) * sxy + (size_t)wrapi(y, m.ny) * m.nx + wrapi(x, m.nx)], v);
+      });
+    }
+  }
+}
+
+
+}  // namespace pmgb

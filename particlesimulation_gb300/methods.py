@@ -377,6 +377,77 @@ class LearnedClosure:
         return float(c.value), (d[0], d[1], d[2])
 
 
+class Ensemble:
+    """Independent PM systems advanced together, one launch per stage (pmgb_ensemble_*).
+    `systems` is a list of dicts with the PMMethod arguments: state, masses, box, H, DT, G,
+    interpolation, finite_diff, greens, diameter, grid, periodic (optional)."""
+
+    def __init__(self, systems):
+        S = len(systems)
+        cfgs = (_lib.PMConfigC * S)()
+        counts = (C.c_int * S)()
+        self._keep = []
+        sp = (C.POINTER(C.c_float) * S)()
+        mp = (C.POINTER(C.c_float) * S)()
+        self.N = []
+        for s, d in enumerate(systems):
+            m = _f32(d["masses"]).reshape(-1)
+            st = _f32(d["state"], (2 * len(m), 3))
+            self._keep += [m, st]
+            c = cfgs[s]
+            c.grid[:] = [int(g) for g in d["grid"]]
+            c.box[:] = [float(b) for b in d["box"]]
+            c.H, c.DT, c.G = float(d["H"]), float(d["DT"]), float(d["G"])
+            c.interpolation, c.finite_diff, c.greens = int(d["interpolation"]), int(d["finite_diff"]), int(d["greens"])
+            c.particle_diameter = float(d.get("diameter", 0.0))
+            c.periodic = int(bool(d.get("periodic", False)))
+            counts[s] = len(m)
+            sp[s] = _fp(st)
+            mp[s] = _fp(m)
+            self.N.append(len(m))
+        h = C.c_void_p()
+        check(lib().pmgb_ensemble_create(S, cfgs, counts, sp, mp, C.byref(h)))
+        self._h = h
+        self.S = S
+
+    def close(self):
+        if getattr(self, "_h", None):
+            check(lib().pmgb_ensemble_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, simLength: int):
+        """(escaped flags per system, device ms)"""
+        esc = (C.c_int * self.S)()
+        ms = C.c_float(0)
+        check(lib().pmgb_ensemble_run(self._h, int(simLength), esc, C.byref(ms)))
+        return [bool(e) for e in esc], float(ms.value)
+
+    def advance(self, nSteps: int) -> float:
+        ms = C.c_float(0)
+        check(lib().pmgb_ensemble_advance(self._h, int(nSteps), C.byref(ms)))
+        return float(ms.value)
+
+    def getParticles(self, system: int, units: str = "code"):
+        n = self.N[system]
+        pos, vel, acc = (np.zeros((n, 3), np.float32) for _ in range(3))
+        u = UNITS_ORIGINAL if units == "original" else UNITS_CODE
+        check(lib().pmgb_ensemble_get_particles(self._h, int(system), _fp(pos), _fp(vel), _fp(acc), u))
+        return pos, vel, acc
+
+    def tuning(self):
+        ppt, mult = C.c_int(0), C.c_int(0)
+        t = np.zeros(6, np.float32)
+        check(lib().pmgb_ensemble_tuning(self._h, C.byref(ppt), C.byref(mult), _fp(t)))
+        return {"deposit_particles_per_thread": ppt.value, "x_rows_mult": mult.value,
+                "candidate_ms": t.tolist()}
+
+
 def mlp_param_count() -> int:
     return int(lib().pmgb_closure_param_count())
 

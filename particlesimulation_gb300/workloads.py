@@ -165,6 +165,30 @@ def disk_p3m_1m(n=1048576, seed=4, grid=128, cutoff_cells=3.0):
     return w
 
 
+def plummer_ensemble(n_systems=64, seed=3, nmin=4096, nmax=131072, steps=100):
+    """C3: independent Plummer systems as plummer_cluster (M=1, a=1, G=1, r <= 10, box 30,
+    CIC, 2-point, discrete Laplacian, dt 0.01), N log-uniform in [nmin, nmax], mesh the power of
+    two in {32, 64, 128} nearest to 2 N^(1/3); returns a list of Workloads."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for s in range(n_systems):
+        n = int(round(np.exp(rng.uniform(np.log(nmin), np.log(nmax)))))
+        target = 2.0 * n ** (1.0 / 3.0)
+        grid = min((32, 64, 128), key=lambda g: abs(np.log2(g) - np.log2(target)))
+        w = plummer_cluster(n=n, seed=int(rng.integers(1 << 31)), grid=grid)
+        w.name = f"plummer_ensemble[{s}]"
+        w.steps = steps
+        out.append(w)
+    return out
+
+
+def as_system(w: Workload) -> dict:
+    """PMMethod arguments of a workload, as particlesimulation_gb300.methods.Ensemble takes them."""
+    return dict(state=w.state, masses=w.mass, box=w.box, H=w.H, DT=w.DT, G=w.G,
+                interpolation=w.interpolation, finite_diff=w.finite_diff, greens=w.greens,
+                diameter=w.diameter, grid=w.grid, periodic=w.periodic)
+
+
 WORKLOADS = {
     "plummer_cluster": plummer_cluster,
     "disk_p3m": disk_p3m,
