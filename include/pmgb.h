@@ -159,6 +159,34 @@ int pmgb_pm_stage_times(pmgb_pm* pm, float* ms5);
 /* Number of particles and the grid of a handle. */
 int pmgb_pm_size(pmgb_pm* pm, int* n, int* grid3);
 
+/* ---------------------------------------------------------------- run diagnostics ---- */
+
+/* What PMMethod::run / P3MMethod::run(..., collectDiagnostics = true) record once per loop
+ * iteration, right after its drift (source/pmMethod.cpp:66-106, source/p3mMethod.cpp:69-130,
+ * source/PMMethodGPU.cu:86-139): the SimInfo quantities of source/simInfo.cpp:50-127, in
+ * original units, summed in double on the device.  One record = PMGB_DIAG_WIDTH doubles: */
+#define PMGB_DIAG_WIDTH 12
+#define PMGB_DIAG_POTENTIAL 0          /* potentialEnergy(density, potential, ...): 0.5 H^3
+                                          sum(rho phi) over the mesh + sum(m Phi_ext(x)) */
+#define PMGB_DIAG_KINETIC 1            /* kineticEnergy: sum(0.5 m |v|^2), half-step v */
+#define PMGB_DIAG_MOMENTUM 2           /* totalMomentum: sum(m u), u = v + a/2 (3 values) */
+#define PMGB_DIAG_ANGULAR_MOMENTUM 5   /* totalAngularMomentum: sum(m x cross u) (3) */
+#define PMGB_DIAG_EXPECTED_MOMENTUM 8  /* initial momentum + DT sum(totalExternalForce) (3) */
+#define PMGB_DIAG_EXTERNAL_POTENTIAL 11 /* the sum(m Phi_ext(x)) part of PMGB_DIAG_POTENTIAL */
+
+/* capacity > 0: record diagnostics during pmgb_pm_run / pmgb_p3m_run / pmgb_pm_advance, keeping
+ * the first `capacity` records (device memory: capacity * 96 bytes plus 4 bytes per mesh cell
+ * for the density copy).  Clears the records and sets the expected momentum to the current
+ * total momentum (SimInfo::setInitialMomentum); pmgb_pm_run does both again when it starts.
+ * With diagnostics on, every iteration also rounds the masses through original units and back
+ * as the reference does (massToOriginalUnits / massToCodeUnits).  capacity = 0: off. */
+int pmgb_pm_set_diagnostics(pmgb_pm* pm, int capacity);
+
+/* Copies min(records taken, capacity, max_records) records into `records` (row-major,
+ * PMGB_DIAG_WIDTH doubles each) and sets *count = records taken since they were last cleared
+ * (records beyond the capacity are dropped).  *count = 0 when diagnostics are off. */
+int pmgb_pm_get_diagnostics(pmgb_pm* pm, double* records, int max_records, int* count);
+
 /* ---------------------------------------------------------------- P3M --------------- */
 
 /* P3MMethod::P3MMethod (source/p3mMethod.cpp:19-48): chaining mesh and short-range force

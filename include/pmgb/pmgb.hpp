@@ -37,6 +37,18 @@ enum class CloudShape { S1 = PMGB_S1, S2 = PMGB_S2 };
 
 // The reference's Particle (include/particle.h:5-15) without the per-neighbour P3M slots,
 // which the device path does not need.
+// One record of the run diagnostics (PMGB_DIAG_* layout of pmgb.h): what SimInfo computes
+// (reference source/simInfo.cpp:50-127) after each drift of a run with collectDiagnostics.
+struct DiagnosticsRecord {
+  double potentialEnergy;
+  double kineticEnergy;
+  double momentum[3];
+  double angularMomentum[3];
+  double expectedMomentum[3];
+  double externalPotentialEnergy;
+};
+static_assert(sizeof(DiagnosticsRecord) == PMGB_DIAG_WIDTH * sizeof(double), "record layout");
+
 struct Particle {
   Vec3 position, velocity, acceleration;
   float mass{};
@@ -107,9 +119,11 @@ class PMMethodGPU {
   PMMethodGPU(const PMMethodGPU&) = delete;
   PMMethodGPU& operator=(const PMMethodGPU&) = delete;
 
-  // PMMethod::run without StateRecorder / diagnostics; returns "" (the reference returns the
-  // recorder's output directory).
-  std::string run(const int simLength) {
+  // PMMethod::run without StateRecorder; returns "" (the reference returns the recorder's
+  // output directory).  collectDiagnostics records the per-iteration diagnostics, read with
+  // diagnostics().
+  std::string run(const int simLength, bool collectDiagnostics = false) {
+    if (collectDiagnostics) ensureDiagnostics(simLength + 1);
     int done = 0;
     int rc = pmgb_pm_run(h, simLength, &done);
     check(rc);
@@ -172,10 +186,28 @@ class PMMethodGPU {
     return d;
   }
 
+  // Records of the last run with collectDiagnostics (or since setDiagnostics), in original
+  // units and double precision.
+  std::vector<DiagnosticsRecord> diagnostics() {
+    std::vector<DiagnosticsRecord> r(static_cast<size_t>(diagCapacity));
+    int taken = 0;
+    check(pmgb_pm_get_diagnostics(h, reinterpret_cast<double*>(r.data()), diagCapacity, &taken));
+    r.resize(size_t(taken < diagCapacity ? taken : diagCapacity));
+    return r;
+  }
+  void setDiagnostics(int capacity) {
+    check(pmgb_pm_set_diagnostics(h, capacity));
+    diagCapacity = capacity;
+  }
+  void ensureDiagnostics(int capacity) {
+    if (diagCapacity < capacity) setDiagnostics(capacity);
+  }
+
   pmgb_pm* handle() { return h; }
 
  private:
   pmgb_pm* h = nullptr;
+  int diagCapacity = 0;
   int N;
   float H, DT, G;
   std::vector<Particle> particles;
@@ -207,7 +239,8 @@ class P3MMethod {
   P3MMethod(const P3MMethod&) = delete;
   P3MMethod& operator=(const P3MMethod&) = delete;
 
-  void run(const int simLength) {
+  void run(const int simLength, bool collectDiagnostics = false) {
+    if (collectDiagnostics) pm.ensureDiagnostics(simLength + 1);
     int done = 0;
     int rc = pmgb_p3m_run(h, simLength, &done);
     check(rc);

@@ -173,20 +173,47 @@ def ref_p3m_accel(cfg: PMConfig, q: P3MConfig, pos, vel, mass):
     return acc
 
 
-def ref_run(cfg: PMConfig, q: P3MConfig | None, pos, vel, mass, sim_length):
+def _read_ref_diagnostics(d):
+    """The text files StateRecorder writes with collectDiagnostics (reference
+    source/stateRecorder.cpp:63-107) as an (R, 12) array in the PMGB_DIAG_* layout; column 11
+    (the external part of the potential energy) is not recorded by the reference: NaN."""
+    def load(name, cols):
+        a = np.loadtxt(os.path.join(d, name), ndmin=2)
+        return a.reshape(-1, cols)
+    e = load("energy.txt", 2)
+    p = load("momentum.txt", 3)
+    la = load("angular_momentum.txt", 3)
+    pe = load("expected_momentum.txt", 3)
+    out = np.full((len(e), 12), np.nan)
+    out[:, 0:2] = e
+    out[:, 2:5] = p
+    out[:, 5:8] = la
+    out[:, 8:11] = pe
+    return out
+
+
+def ref_run(cfg: PMConfig, q: P3MConfig | None, pos, vel, mass, sim_length, diagnostics=False):
+    """PMMethod::run / P3MMethod::run of the compiled reference; with diagnostics=True also
+    returns the recorded energy / momentum records (see _read_ref_diagnostics)."""
     n = len(mass)
     st, m = _state(pos, vel), _f32(mass)
     out = np.zeros((2 * n, 3), np.float32)
     esc = C.c_int(0)
+    diag = None
     with tempfile.TemporaryDirectory() as d:
         if q is None:
             rc = ref().ref_pm_run(C.byref(cfg.c()), n, _ptr(st, C.c_float), _ptr(m, C.c_float),
-                                  sim_length, d.encode(), _ptr(out, C.c_float), C.byref(esc))
+                                  sim_length, d.encode(), _ptr(out, C.c_float), C.byref(esc),
+                                  int(diagnostics))
         else:
             rc = ref().ref_p3m_run(C.byref(cfg.c()), C.byref(q.c()), n, _ptr(st, C.c_float),
                                    _ptr(m, C.c_float), sim_length, d.encode(),
-                                   _ptr(out, C.c_float), C.byref(esc))
+                                   _ptr(out, C.c_float), C.byref(esc), int(diagnostics))
+        if rc == 0 and diagnostics:
+            diag = _read_ref_diagnostics(d)
     assert rc == 0
+    if diagnostics:
+        return out[:n], out[n:], bool(esc.value), diag
     return out[:n], out[n:], bool(esc.value)
 
 
@@ -252,19 +279,28 @@ def port_p3m_accel(cfg: PMConfig, q: P3MConfig, pos, vel, mass, prec=1, nthreads
 
 
 def port_run(cfg: PMConfig, q: P3MConfig | None, pos, vel, mass, sim_length, prec=1,
-             nthreads=None):
+             nthreads=None, diagnostics=False):
+    """The port's run loop; with diagnostics=True also returns the (R, 12) FP64 records of the
+    reference's collectDiagnostics (layout of include/pmgb.h's PMGB_DIAG_*)."""
     n = len(mass)
     st, m = _state(pos, vel), _f32(mass)
     out = np.zeros((2 * n, 3), np.float64)
     esc = C.c_int(0)
+    cap = sim_length + 1 if diagnostics else 0
+    diag = np.zeros((max(cap, 1), 12), np.float64)
+    cnt = C.c_int(0)
+    dptr = _ptr(diag, C.c_double) if diagnostics else C.POINTER(C.c_double)()
     if q is None:
         rc = port().port_pm_run(prec, C.byref(cfg.c()), n, _ptr(st, C.c_float), _ptr(m, C.c_float),
-                                sim_length, _ptr(out, C.c_double), C.byref(esc))
+                                sim_length, _ptr(out, C.c_double), C.byref(esc), dptr, cap,
+                                C.byref(cnt))
     else:
         rc = port().port_p3m_run(prec, C.byref(cfg.c()), C.byref(q.c()), n, _ptr(st, C.c_float),
                                  _ptr(m, C.c_float), sim_length, _ptr(out, C.c_double),
-                                 C.byref(esc), nthreads or os.cpu_count())
+                                 C.byref(esc), nthreads or os.cpu_count(), dptr, cap, C.byref(cnt))
     assert rc == 0
+    if diagnostics:
+        return out[:n], out[n:], bool(esc.value), diag[: min(cnt.value, cap)].copy()
     return out[:n], out[n:], bool(esc.value)
 
 

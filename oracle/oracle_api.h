@@ -64,11 +64,15 @@ int ref_pm_accel(const orc_pm_params* p, int n, const float* state, const float*
                  float* acc, float* density, float* potential, float* green);
 int ref_p3m_accel(const orc_pm_params* p, const orc_p3m_params* q, int n, const float* state,
                   const float* masses, float* acc);
+/* run(recorder, sim_length, collect_diagnostics, false) with a StateRecorder writing into
+ * outdir (positions.dat, energy.txt, momentum.txt, expected_momentum.txt,
+ * angular_momentum.txt). */
 int ref_pm_run(const orc_pm_params* p, int n, const float* state, const float* masses,
-               int sim_length, const char* outdir, float* state_out, int* escaped);
+               int sim_length, const char* outdir, float* state_out, int* escaped,
+               int collect_diagnostics);
 int ref_p3m_run(const orc_pm_params* p, const orc_p3m_params* q, int n, const float* state,
                 const float* masses, int sim_length, const char* outdir, float* state_out,
-                int* escaped);
+                int* escaped, int collect_diagnostics);
 /* Chaining-mesh cell lists: order[] = particle ids cell by cell, counts[] = list length
  * per cell, dims[3] = (Mx, My, Mz).  pos_code = N xyz triplets in code units. */
 int ref_chaining_mesh(const orc_p3m_params* q, float H, int n, const float* pos_code,
@@ -84,11 +88,15 @@ int port_pm_accel(int prec, const orc_pm_params* p, int n, const float* state,
 int port_p3m_accel(int prec, const orc_pm_params* p, const orc_p3m_params* q, int n,
                    const float* state, const float* masses, double* acc, double* acc_sr,
                    int nthreads);
+/* Run loops.  diag != NULL turns on the reference's collectDiagnostics: one record of 12
+ * doubles per loop iteration (layout of include/pmgb.h's PMGB_DIAG_*), at most diag_cap of
+ * them stored; *diag_count = records taken. */
 int port_pm_run(int prec, const orc_pm_params* p, int n, const float* state,
-                const float* masses, int sim_length, double* state_out, int* escaped);
+                const float* masses, int sim_length, double* state_out, int* escaped,
+                double* diag, int diag_cap, int* diag_count);
 int port_p3m_run(int prec, const orc_pm_params* p, const orc_p3m_params* q, int n,
                  const float* state, const float* masses, int sim_length, double* state_out,
-                 int* escaped, int nthreads);
+                 int* escaped, int nthreads, double* diag, int diag_cap, int* diag_count);
 int port_chaining_mesh(const orc_p3m_params* q, float H, int n, const float* pos_code,
                        int y_sorting, int* order, int* counts, int* dims);
 /* FP64 direct sum (ppMethod.cpp:23-36 restated in double) for the targets idx[0..m):

@@ -469,8 +469,11 @@ struct PM {
     V3<T> f = g * dir;
     return (DT * DT * f) / H;
   }
+  std::vector<T> rhoReal;  // density of the last step (the FFT below overwrites dens)
   void step() {  // pmMethodStep (pmMethod.cpp:137-144)
     spreadMass();
+    rhoReal.resize(L);
+    for (size_t id = 0; id < L; ++id) rhoReal[id] = dens[id].real();
     fft.run(dens, false, nthreads);
     potF = dens;
     for (size_t id = 0; id < L; ++id) potF[id] = dens[id] * std::complex<T>(green[id], 0);
@@ -685,9 +688,90 @@ void exportState(PM<T>& pm, bool codeUnits, double* out) {
   }
 }
 
-// PMMethod::run / P3MMethod::run without diagnostics or recording (pmMethod.cpp:62-135).
+/* ------------------------------------------------------------ diagnostics ---- */
+// The quantities SimInfo computes (source/simInfo.cpp:50-127) at the point of the run loop
+// where PMMethod::run / P3MMethod::run record them with collectDiagnostics
+// (source/pmMethod.cpp:66-106, source/p3mMethod.cpp:69-130), every sum in double.  One record
+// is 12 doubles, the layout of the C ABI's PMGB_DIAG_* indices:
+//   0 potential energy  0.5 H^3 sum(rho_orig phi_orig) + sum(m Phi_ext(x))
+//   1 kinetic energy    sum(0.5 m |v|^2), v = the half-step velocity
+//   2-4 momentum        sum(m u), u = integer-step velocity v + a/2
+//   5-7 angular mom.    sum(m x cross u)
+//   8-10 expected mom.  initial momentum + DT sum over records of sum(m g_ext(x))
+//   11 external part    sum(m Phi_ext(x))
+struct DiagOut {
+  double* out = nullptr;
+  int cap = 0;
+  int count = 0;
+  double pexp[3] = {0, 0, 0};
+};
+
+// sphRadDecrField / sphRadDecrFieldPotential (source/externalFields.cpp:4-28) in double.
+void extFieldPot(const orc_pm_params& p, double x, double y, double z, double g[3], double* phi) {
+  g[0] = g[1] = g[2] = 0;
+  *phi = 0;
+  if (p.ext_kind != 1) return;
+  const double dx = x - p.ext_cx, dy = y - p.ext_cy, dz = z - p.ext_cz;
+  const double r = std::sqrt(dx * dx + dy * dy + dz * dz);
+  const double R = p.ext_R, M = p.ext_M, G = p.ext_G;
+  const double gm = r > R ? -G * M / (r * r) : -(G * M / (R * R * R)) * r * (4 - 3 * r / R);
+  if (r > 0) {
+    g[0] = gm * dx / r;
+    g[1] = gm * dy / r;
+    g[2] = gm * dz / r;
+  }
+  const double u = r / R;
+  *phi = r > R ? -G * M / r : G * M / R * (-2 + u * u * (2 - u));
+}
+
+// One record; pm.x, pm.v, pm.m and isv are in original units at this point of the loop.
 template <typename T>
-void runLoop(PM<T>& pm, P3M<T>* p3m, int simLength, double* out, int* escaped) {
+void diagRecord(const PM<T>& pm, const std::vector<V3<T>>& isv, DiagOut& d) {
+  double ke = 0, P[3] = {0, 0, 0}, Lm[3] = {0, 0, 0}, F[3] = {0, 0, 0}, U = 0;
+  for (int i = 0; i < pm.N; ++i) {
+    const double m = pm.m[i];
+    const double x = pm.x[i].x, y = pm.x[i].y, z = pm.x[i].z;
+    const double vx = pm.v[i].x, vy = pm.v[i].y, vz = pm.v[i].z;
+    const double ux = isv[i].x, uy = isv[i].y, uz = isv[i].z;
+    ke += 0.5 * m * (vx * vx + vy * vy + vz * vz);
+    P[0] += m * ux;
+    P[1] += m * uy;
+    P[2] += m * uz;
+    Lm[0] += m * (y * uz - z * uy);
+    Lm[1] += m * (z * ux - x * uz);
+    Lm[2] += m * (x * uy - y * ux);
+    double g[3], phi;
+    extFieldPot(pm.p, x, y, z, g, &phi);
+    F[0] += m * g[0];
+    F[1] += m * g[1];
+    F[2] += m * g[2];
+    U += m * phi;
+  }
+  double mesh = 0;
+  for (size_t id = 0; id < pm.L; ++id) mesh += double(pm.rhoReal[id]) * double(pm.pot[id].real());
+  const double H = pm.p.H, DT = pm.p.DT, G = pm.p.G;
+  const double kr = 1.0 / (DT * DT * 4 * std::numbers::pi * G), kp = H * H / (DT * DT);
+  const double pe = 0.5 * (H * H * H) * mesh * kr * kp + U;
+  for (int c = 0; c < 3; ++c) d.pexp[c] += DT * F[c];
+  if (d.count < d.cap) {
+    double* r = d.out + 12 * size_t(d.count);
+    r[0] = pe;
+    r[1] = ke;
+    for (int c = 0; c < 3; ++c) {
+      r[2 + c] = P[c];
+      r[5 + c] = Lm[c];
+      r[8 + c] = d.pexp[c];
+    }
+    r[11] = U;
+  }
+  ++d.count;
+}
+
+// PMMethod::run / P3MMethod::run without recording, with the diagnostics when diag != null
+// (pmMethod.cpp:62-135, p3mMethod.cpp:59-166).
+template <typename T>
+void runLoop(PM<T>& pm, P3M<T>* p3m, int simLength, double* out, int* escaped,
+             DiagOut* diag = nullptr) {
   auto force = [&]() {
     pm.step();
     if (p3m) {
@@ -695,6 +779,14 @@ void runLoop(PM<T>& pm, P3M<T>* p3m, int simLength, double* out, int* escaped) {
       p3m->correct();
     }
   };
+  std::vector<V3<T>> isv;
+  if (diag) {  // setInitialMomentum: integerStepVelocity == velocity at construction
+    isv.resize(pm.N);
+    for (int i = 0; i < pm.N; ++i)
+      for (int c = 0; c < 3; ++c)
+        diag->pexp[c] += double(pm.m[i]) * double(c == 0 ? pm.v[i].x : c == 1 ? pm.v[i].y : pm.v[i].z);
+  }
+  const T H = pm.H, DT = pm.DT, G = pm.G;
   pm.toCode();
   pm.initGreen();
   force();
@@ -702,13 +794,21 @@ void runLoop(PM<T>& pm, P3M<T>* p3m, int simLength, double* out, int* escaped) {
   *escaped = 0;
   for (int t = 0; t <= simLength; ++t) {
     for (int i = 0; i < pm.N; ++i) pm.x[i] += pm.v[i];  // updatePositions
+    if (diag)  // setIntegerStepVelocities, integerStepVelocitiesToOriginalUnits
+      for (int i = 0; i < pm.N; ++i) isv[i] = (H * (pm.v[i] + T(0.5) * pm.a[i])) / DT;
     pm.statesToOriginal();
+    if (diag) {
+      for (int i = 0; i < pm.N; ++i) pm.m[i] = (H * H * H) / (DT * DT * 4 * PI<T> * G) * pm.m[i];
+      diagRecord(pm, isv, *diag);
+    }
     if (pm.escaped()) {
       *escaped = 1;
       exportState(pm, false, out);
       return;
     }
     pm.statesToCode();
+    if (diag)
+      for (int i = 0; i < pm.N; ++i) pm.m[i] = DT * DT * 4 * PI<T> * G / (H * H * H) * pm.m[i];
     force();
     for (int i = 0; i < pm.N; ++i) pm.v[i] += pm.a[i];  // updateVelocities
   }
@@ -781,29 +881,40 @@ int port_p3m_accel(int prec, const orc_pm_params* p, const orc_p3m_params* q, in
 }
 
 int port_pm_run(int prec, const orc_pm_params* p, int n, const float* state,
-                const float* masses, int sim_length, double* state_out, int* escaped) {
+                const float* masses, int sim_length, double* state_out, int* escaped,
+                double* diag, int diag_cap, int* diag_count) {
+  DiagOut d;
+  d.out = diag;
+  d.cap = diag ? diag_cap : 0;
+  DiagOut* dp = diag ? &d : nullptr;
   if (prec) {
     PM<double> pm(p, n, state, masses, 1);
-    runLoop<double>(pm, nullptr, sim_length, state_out, escaped);
+    runLoop<double>(pm, nullptr, sim_length, state_out, escaped, dp);
   } else {
     PM<float> pm(p, n, state, masses, 1);
-    runLoop<float>(pm, nullptr, sim_length, state_out, escaped);
+    runLoop<float>(pm, nullptr, sim_length, state_out, escaped, dp);
   }
+  if (diag_count) *diag_count = d.count;
   return 0;
 }
 
 int port_p3m_run(int prec, const orc_pm_params* p, const orc_p3m_params* q, int n,
                  const float* state, const float* masses, int sim_length, double* state_out,
-                 int* escaped, int nthreads) {
+                 int* escaped, int nthreads, double* diag, int diag_cap, int* diag_count) {
+  DiagOut d;
+  d.out = diag;
+  d.cap = diag ? diag_cap : 0;
+  DiagOut* dp = diag ? &d : nullptr;
   if (prec) {
     PM<double> pm(p, n, state, masses, 1);
     P3M<double> p3m(q, pm, nthreads);
-    runLoop<double>(pm, &p3m, sim_length, state_out, escaped);
+    runLoop<double>(pm, &p3m, sim_length, state_out, escaped, dp);
   } else {
     PM<float> pm(p, n, state, masses, 1);
     P3M<float> p3m(q, pm, nthreads);
-    runLoop<float>(pm, &p3m, sim_length, state_out, escaped);
+    runLoop<float>(pm, &p3m, sim_length, state_out, escaped, dp);
   }
+  if (diag_count) *diag_count = d.count;
   return 0;
 }
 

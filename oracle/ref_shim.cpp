@@ -203,7 +203,8 @@ int ref_p3m_accel(const orc_pm_params* p, const orc_p3m_params* q, int n, const 
 }
 
 int ref_pm_run(const orc_pm_params* p, int n, const float* state, const float* masses,
-               int sim_length, const char* outdir, float* state_out, int* escaped) {
+               int sim_length, const char* outdir, float* state_out, int* escaped,
+               int collect_diagnostics) {
   try {
     PMBundle b = makePM(p, n, state, masses);
     {
@@ -211,7 +212,7 @@ int ref_pm_run(const orc_pm_params* p, int n, const float* state, const float* m
       std::streambuf* old = std::cout.rdbuf();
       std::ostringstream sink;
       std::cout.rdbuf(sink.rdbuf());
-      b.pm->run(rec, sim_length, false, false);
+      b.pm->run(rec, sim_length, collect_diagnostics != 0, false);
       std::cout.rdbuf(old);
     }
     exportRunState(b.pm->getParticles(), p, outdir, n, state_out, escaped);
@@ -224,7 +225,7 @@ int ref_pm_run(const orc_pm_params* p, int n, const float* state, const float* m
 
 int ref_p3m_run(const orc_pm_params* p, const orc_p3m_params* q, int n, const float* state,
                 const float* masses, int sim_length, const char* outdir, float* state_out,
-                int* escaped) {
+                int* escaped, int collect_diagnostics) {
   try {
     PMBundle b = makePM(p, n, state, masses);
     P3MMethod p3m(*b.pm, std::make_tuple(q->comp_x, q->comp_y, q->comp_z), q->cutoff,
@@ -235,7 +236,7 @@ int ref_p3m_run(const orc_pm_params* p, const orc_p3m_params* q, int n, const fl
       std::streambuf* old = std::cout.rdbuf();
       std::ostringstream sink;
       std::cout.rdbuf(sink.rdbuf());
-      p3m.run(rec, sim_length, false, false);
+      p3m.run(rec, sim_length, collect_diagnostics != 0, false);
       std::cout.rdbuf(old);
     }
     exportRunState(b.pm->getParticles(), p, outdir, n, state_out, escaped);

@@ -12,13 +12,15 @@ LIB_PATH = os.path.join(PKG, "libpmgb.so")
 
 PMGB_OK, PMGB_EINVAL, PMGB_ECUDA, PMGB_EESCAPED, PMGB_ETIMEOUT, PMGB_ENOMEM = range(6)
 UNITS_CODE, UNITS_ORIGINAL = 0, 1
+DIAG_WIDTH = 12  # PMGB_DIAG_WIDTH
 
 # Every symbol declared in include/pmgb.h (checked by tests/test_abi.py).
 EXPORTS = [
     "pmgb_pm_create", "pmgb_pm_destroy", "pmgb_pm_init_greens_function", "pmgb_pm_method_step",
     "pmgb_pm_run", "pmgb_pm_advance", "pmgb_pm_get_particles", "pmgb_pm_set_particles", "pmgb_pm_escaped",
     "pmgb_pm_get_density", "pmgb_pm_get_potential", "pmgb_pm_get_greens_function",
-    "pmgb_pm_stage_times", "pmgb_pm_size", "pmgb_p3m_create", "pmgb_p3m_destroy",
+    "pmgb_pm_stage_times", "pmgb_pm_size", "pmgb_pm_set_diagnostics", "pmgb_pm_get_diagnostics",
+    "pmgb_p3m_create", "pmgb_p3m_destroy",
     "pmgb_p3m_force", "pmgb_p3m_run", "pmgb_p3m_get_cell_lists", "pmgb_p3m_get_sr_table",
     "pmgb_p3m_pair_count", "pmgb_fp32_peak_probe", "pmgb_kernel_launches",
     "pmgb_chaining_mesh_fill_noalloc", "pmgb_p3m_set_pair_counting",
@@ -83,6 +85,8 @@ def lib() -> C.CDLL:
         L.pmgb_pm_get_greens_function.argtypes = [vp, fp]
         L.pmgb_pm_stage_times.argtypes = [vp, fp]
         L.pmgb_pm_size.argtypes = [vp, ip, ip]
+        L.pmgb_pm_set_diagnostics.argtypes = [vp, C.c_int]
+        L.pmgb_pm_get_diagnostics.argtypes = [vp, C.POINTER(C.c_double), C.c_int, ip]
         L.pmgb_p3m_create.argtypes = [vp, C.POINTER(P3MConfigC), C.POINTER(vp)]
         L.pmgb_p3m_destroy.argtypes = [vp]
         L.pmgb_p3m_force.argtypes = [vp]

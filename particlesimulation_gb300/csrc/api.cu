@@ -54,7 +54,8 @@ int dalloc(T** p, size_t count) {
 
 void free_pm(pmgb_pm* h) {
   if (!h) return;
-  void* ptrs[] = {h->pm[0], h->pm[1], h->vi[0], h->vi[1], h->acc,  h->acc_pm, h->keys, h->keys_alt,
+  diag_free(h);
+  void* ptrs[]= {h->pm[0], h->pm[1], h->vi[0], h->vi[1], h->acc,  h->acc_pm, h->keys, h->keys_alt,
                   h->vals,  h->vals_alt, h->hist, h->rho, h->spec, h->phi, h->ghat, h->tw, h->flags,
                   h->stage, h->mass_code};
   for (void* p : ptrs)
@@ -159,7 +160,8 @@ int force(pmgb_pm* h, int kdk, float kick, int drift, int tag, bool timed) {
   rc = launch_deposit(h->cfg.interpolation, h->pm[h->cur], n, h->m, h->sp.fx_scale, h->rho, stop, h->st);
   if (rc) return rc;
   if (timed) cudaEventRecord(h->ev[2], h->st);
-  rc = launch_poisson(h->rho, h->spec, h->phi, h->ghat, h->tw, h->nmax, h->m, h->sp.fx_inv, stop, h->st);
+  rc = launch_poisson(h->rho, h->spec, h->phi, h->ghat, h->tw, h->nmax, h->m, h->sp.fx_inv, stop, h->st,
+                      diag_density(h));
   if (rc) return rc;
   if (timed) cudaEventRecord(h->ev[3], h->st);
   StepParams sp = h->sp;
@@ -199,12 +201,17 @@ int run_loop(pmgb_pm* h, int sim_length, int* steps_done) {
   PMGB_CUDA_TRY(cudaMemsetAsync(h->flags, 0, sizeof(int), h->st));
   const int big = 0x7FFFFFFF;
   PMGB_CUDA_TRY(cudaMemcpyAsync(h->flags + 1, &big, sizeof(int), cudaMemcpyHostToDevice, h->st));
+  int rc = diag_run_begin(h);
+  if (rc) return rc;
   // initial force, half kick (setHalfStepVelocities) and the drift of iteration 0
-  int rc = force(h, 1, 0.5f, 1, 0, false);
+  rc = force(h, 1, 0.5f, 1, 0, false);
+  if (rc) return rc;
+  rc = diag_after_drift(h, 0);
   if (rc) return rc;
   for (int t = 0; t <= sim_length; ++t) {
     rc = force(h, 1, 1.0f, t < sim_length ? 1 : 0, t + 1, false);
     if (rc) return rc;
+    if (t < sim_length && (rc = diag_after_drift(h, t + 1))) return rc;
   }
   int flags[2];
   PMGB_CUDA_TRY(cudaMemcpyAsync(flags, h->flags, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
@@ -402,11 +409,15 @@ int pmgb_pm_advance(pmgb_pm* h, int n_steps, int* steps_done, float* device_ms) 
     // the first drift of the loop body, then (force, kick, drift) with the last drift left out
     StepParams sp = h->sp;
     sp.step_tag = 0;
-    int rc = launch_kick_drift(h->pm[h->cur], h->vi[h->cur], h->acc, h->n, sp, 0.f, 1, h->flags, h->st);
+    int rc = diag_before_drift(h);
     if (rc) return rc;
+    rc = launch_kick_drift(h->pm[h->cur], h->vi[h->cur], h->acc, h->n, sp, 0.f, 1, h->flags, h->st);
+    if (rc) return rc;
+    if ((rc = diag_after_drift(h, 0))) return rc;
     for (int t = 0; t < n_steps; ++t) {
       rc = force(h, 1, 1.0f, t + 1 < n_steps ? 1 : 0, t + 1, false);
       if (rc) return rc;
+      if (t + 1 < n_steps && (rc = diag_after_drift(h, t + 1))) return rc;
     }
   }
   PMGB_CUDA_TRY(cudaEventRecord(h->ev[5], h->st));

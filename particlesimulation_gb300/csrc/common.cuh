@@ -61,6 +61,14 @@ struct StepParams {
   int periodic;       // wrap positions into the mesh after a drift instead of the escape test
 };
 
+// Entry test of a kernel that may drift.  A drift that escapes sets stop[0] while other blocks
+// of the same launch may not have started yet, so such a kernel must not test stop[0]: it
+// stops only if an earlier iteration escaped (stop[1] holds the smallest escaping iteration,
+// INT_MAX at the start of a run).  Every other kernel tests stop[0].
+__device__ __forceinline__ bool stopped_before(const int* stop, bool drifts, int tag) {
+  return drifts ? stop[1] < tag : stop[0] != 0;
+}
+
 // Kick, drift, the reference's unit round trip (stateToOriginalUnits / stateToCodeUnits,
 // source/pmMethod.cpp:87-113) and the escapedComputationalBox test (146-156) of one particle,
 // dt = 1 in code units (source/leapfrog.cpp:5-24).  An escape sets stop[0] and records the

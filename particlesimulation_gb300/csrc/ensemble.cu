@@ -32,17 +32,29 @@ struct EnsSys {
   StepParams sp;
 };
 
+// Escape flags, 4 ints per system: [0] committed stop, [1] unused, [2] pending stop and [3] its
+// iteration, written by kick_drift in the interpolation kernel.  A drifting launch tests only the
+// committed word, so an escape in one of its blocks does not make the blocks that start later
+// skip their particles; every other kernel tests both words, and the next step's deposit
+// commits the pending word.
+__device__ __forceinline__ bool ens_stopped(const int* flags, int s) {
+  return (flags[4 * s] | flags[4 * s + 2]) != 0;
+}
+
 template <int IS, int PPT>
 __global__ void __launch_bounds__(DEP_THREADS) ens_deposit_kernel(const EnsSys* __restrict__ sys,
                                                                   const int2* __restrict__ items,
                                                                   int nitems, const float4* __restrict__ pm,
                                                                   u64* __restrict__ rho,
-                                                                  const int* __restrict__ flags) {
+                                                                  int* __restrict__ flags) {
   __shared__ u64 tile[DEP_TILE];
   __shared__ int red[DEP_THREADS / 32];
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const int2 w = items[it];
-    if (flags[2 * w.x]) continue;
+    if (ens_stopped(flags, w.x)) {
+      if (threadIdx.x == 0) flags[4 * w.x] = 1;
+      continue;
+    }
     const EnsSys s = sys[w.x];
     deposit_block<IS, PPT>(pm + s.p_off, w.y, s.n, s.sp.m, s.sp.fx_scale, rho + s.rho_off, tile, red);
     __syncthreads();
@@ -58,7 +70,7 @@ __global__ void __launch_bounds__(FFT_THREADS) ens_fft_x_r2c_kernel(const EnsSys
   extern __shared__ float2 sm[];
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const int2 w = items[it];
-    if (flags[2 * w.x]) continue;
+    if (ens_stopped(flags, w.x)) continue;
     const EnsSys s = sys[w.x];
     fft_x_r2c_body(sm, rho + s.rho_off, spec + s.spec_off, s.sp.m, s.pairs, s.sp.fx_inv, tw, nmax, w.y);
     __syncthreads();
@@ -75,7 +87,7 @@ __global__ void __launch_bounds__(FFT_THREADS) ens_fft_x_c2r_kernel(const EnsSys
   extern __shared__ float2 sm[];
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const int2 w = items[it];
-    if (flags[2 * w.x]) continue;
+    if (ens_stopped(flags, w.x)) continue;
     const EnsSys s = sys[w.x];
     fft_x_c2r_body(sm, spec + s.spec_off, phi + s.rho_off, s.sp.m, s.pairs, tw, nmax, w.y);
     __syncthreads();
@@ -93,7 +105,7 @@ __global__ void __launch_bounds__(FFT_THREADS) ens_fft_cols_kernel(const EnsSys*
   extern __shared__ float2 sm[];
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const int4 w = items[it];
-    if (flags[2 * w.x]) continue;
+    if (ens_stopped(flags, w.x)) continue;
     const EnsSys s = sys[w.x];
     fft_cols_body(sm, spec + s.spec_off, s.sp.m, axis, mode, ghat ? ghat + s.spec_off : nullptr, tw, nmax,
                   w.y, w.z);
@@ -110,8 +122,8 @@ __global__ void __launch_bounds__(256) ens_interp_kernel(const EnsSys* __restric
                                                          int drift, int kdk, int* flags) {
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const int2 w = items[it];
-    int* stop = flags + 2 * w.x;
-    if (*stop) continue;
+    if (kdk && drift ? flags[4 * w.x] != 0 : ens_stopped(flags, w.x)) continue;
+    int* stop = flags + 4 * w.x + 2;
     const EnsSys s = sys[w.x];
     const int i = w.y + threadIdx.x;
     if (i < s.n) {
@@ -162,7 +174,7 @@ struct pmgb_ensemble {
   float* ghat = nullptr;
   float2* tw = nullptr;
   int nmax = 0;
-  int* flags = nullptr;  // 2 per system
+  int* flags = nullptr;  // 4 per system (ens_stopped)
   float* stage = nullptr;
   long long rho_total = 0, spec_total = 0;
   int2* part_items = nullptr;
@@ -518,7 +530,7 @@ int pmgb_ensemble_create(int n_systems, const pmgb_pm_config* cfgs, const int* c
   if ((rc = ens_alloc(&e->sys, n_systems)) || (rc = ens_alloc(&e->pm, NN)) || (rc = ens_alloc(&e->vi, NN)) ||
       (rc = ens_alloc(&e->acc, NN)) || (rc = ens_alloc(&e->rho, rho_off)) || (rc = ens_alloc(&e->spec, spec_off)) ||
       (rc = ens_alloc(&e->phi, rho_off)) || (rc = ens_alloc(&e->ghat, spec_off)) ||
-      (rc = ens_alloc(&e->tw, e->nmax / 2 + 1)) || (rc = ens_alloc(&e->flags, 2 * n_systems)) ||
+      (rc = ens_alloc(&e->tw, e->nmax / 2 + 1)) || (rc = ens_alloc(&e->flags, 4 * n_systems)) ||
       (rc = ens_alloc(&e->stage, 9 * NN)))
     return fail(rc);
   if (cudaMemcpy(e->pm, hp.data(), hp.size() * sizeof(float4), cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -526,7 +538,7 @@ int pmgb_ensemble_create(int n_systems, const pmgb_pm_config* cfgs, const int* c
       cudaMemset(e->acc, 0, NN * sizeof(float4)) != cudaSuccess ||
       cudaMemset(e->rho, 0, rho_off * sizeof(u64)) != cudaSuccess ||
       cudaMemset(e->spec, 0, spec_off * sizeof(float2)) != cudaSuccess ||
-      cudaMemset(e->flags, 0, 2 * n_systems * sizeof(int)) != cudaSuccess)
+      cudaMemset(e->flags, 0, 4 * n_systems * sizeof(int)) != cudaSuccess)
     return set_error("ensemble upload failed"), fail(PMGB_ECUDA);
   {
     std::vector<float2> tw(e->nmax / 2 + 1);
@@ -569,20 +581,21 @@ int pmgb_ensemble_destroy(pmgb_ensemble* e) {
 // iterations; a system whose particle leaves its box stops there, the others go on).
 int pmgb_ensemble_run(pmgb_ensemble* e, int sim_length, int* escaped, float* device_ms) {
   if (!e || sim_length < 0) return set_error("bad argument"), PMGB_EINVAL;
-  PMGB_CUDA_TRY(cudaMemsetAsync(e->flags, 0, 2 * e->S * sizeof(int), e->st));
+  PMGB_CUDA_TRY(cudaMemsetAsync(e->flags, 0, 4 * e->S * sizeof(int), e->st));
   PMGB_CUDA_TRY(cudaEventRecord(e->ev0, e->st));
   PMGB_CUDA_TRY(cudaGraphLaunch(e->graph[0], e->st));
   for (int t = 0; t <= sim_length; ++t) PMGB_CUDA_TRY(cudaGraphLaunch(e->graph[t < sim_length ? 1 : 2], e->st));
   count_launches(7 * (sim_length + 2));
   PMGB_CUDA_TRY(cudaEventRecord(e->ev1, e->st));
-  std::vector<int> flags(2 * e->S);
+  std::vector<int> flags(4 * e->S);
   PMGB_CUDA_TRY(cudaMemcpyAsync(flags.data(), e->flags, flags.size() * sizeof(int), cudaMemcpyDeviceToHost, e->st));
   PMGB_CUDA_TRY(cudaStreamSynchronize(e->st));
   if (device_ms) cudaEventElapsedTime(device_ms, e->ev0, e->ev1);
   bool any = false;
   for (int s = 0; s < e->S; ++s) {
-    if (escaped) escaped[s] = flags[2 * s];
-    any = any || flags[2 * s];
+    const int esc = (flags[4 * s] | flags[4 * s + 2]) != 0;
+    if (escaped) escaped[s] = esc;
+    any = any || esc;
   }
   return any ? PMGB_EESCAPED : PMGB_OK;
 }

@@ -28,10 +28,11 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_x_r2c_kernel(u64* __restrict_
                                                                 float fx_inv,
                                                                 const float2* __restrict__ twg,
                                                                 int nmax,
-                                                                const int* __restrict__ stop) {
+                                                                const int* __restrict__ stop,
+                                                                float* __restrict__ rho_copy) {
   if (stop && *stop) return;
   extern __shared__ float2 sm[];
-  fft_x_r2c_body(sm, rho, spec, m, pairs, fx_inv, twg, nmax, 2ll * blockIdx.x * pairs);
+  fft_x_r2c_body(sm, rho, spec, m, pairs, fx_inv, twg, nmax, 2ll * blockIdx.x * pairs, rho_copy);
 }
 
 __global__ void __launch_bounds__(FFT_THREADS) fft_x_c2r_kernel(const float2* __restrict__ spec,
@@ -76,16 +77,17 @@ int fft_configure(const MeshDims& m) {
   return PMGB_OK;
 }
 
-// density (fixed point, cleared) -> potential
+// density (fixed point, cleared) -> potential; rho_copy (optional) receives the float density
 int launch_poisson(u64* rho, float2* spec, float* phi, const float* ghat, const float2* tw,
-                   int nmax, MeshDims m, float fx_inv, const int* stop, cudaStream_t st) {
+                   int nmax, MeshDims m, float fx_inv, const int* stop, cudaStream_t st,
+                   float* rho_copy) {
   const int pairs = x_pairs(m);
   const int xblocks = (int)((long long)m.ny * m.nz / 2 / pairs);
   const int xsmem = (pairs * m.nx + m.nx / 2) * (int)sizeof(float2);
   const int ctiles = (m.nxp + COL_TX - 1) / COL_TX;
   const int ysmem = (m.ny * COL_TX + m.ny / 2) * (int)sizeof(float2);
   const int zsmem = (m.nz * COL_TX + m.nz / 2) * (int)sizeof(float2);
-  fft_x_r2c_kernel<<<xblocks, FFT_THREADS, xsmem, st>>>(rho, spec, m, pairs, fx_inv, tw, nmax, stop);
+  fft_x_r2c_kernel<<<xblocks, FFT_THREADS, xsmem, st>>>(rho, spec, m, pairs, fx_inv, tw, nmax, stop, rho_copy);
   fft_cols_kernel<<<dim3(ctiles, m.nz), FFT_THREADS, ysmem, st>>>(spec, m, 1, 0, nullptr, tw, nmax, stop);
   fft_cols_kernel<<<dim3(ctiles, m.ny), FFT_THREADS, zsmem, st>>>(spec, m, 2, 2, ghat, tw, nmax, stop);
   fft_cols_kernel<<<dim3(ctiles, m.nz), FFT_THREADS, ysmem, st>>>(spec, m, 1, 1, nullptr, tw, nmax, stop);

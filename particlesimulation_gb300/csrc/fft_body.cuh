@@ -64,11 +64,13 @@ __device__ __forceinline__ void load_twiddles(float2* tws, const float2* twg, in
 }
 
 // ---------------------------------------------------------------- x pass, forward ----
+// rho_copy != nullptr also keeps the float density (the run diagnostics' mesh energy).
 __device__ __forceinline__ void fft_x_r2c_body(float2* sm, u64* __restrict__ rho,
                                                float2* __restrict__ spec, const MeshDims& m,
                                                int pairs, float fx_inv,
                                                const float2* __restrict__ twg, int nmax,
-                                               long long row0) {
+                                               long long row0,
+                                               float* __restrict__ rho_copy = nullptr) {
   const int nx = m.nx;
   float2* tw = sm + pairs * nx;
   load_twiddles(tw, twg, nx, nmax);
@@ -78,7 +80,12 @@ __device__ __forceinline__ void fft_x_r2c_body(float2* sm, u64* __restrict__ rho
     const long long va = (long long)rho[a], vb = (long long)rho[a + nx];
     rho[a] = 0ull;
     rho[a + nx] = 0ull;
-    sm[p * nx + brev(j, m.lx)] = make_float2(__ll2float_rn(va) * fx_inv, __ll2float_rn(vb) * fx_inv);
+    const float2 d = make_float2(__ll2float_rn(va) * fx_inv, __ll2float_rn(vb) * fx_inv);
+    if (rho_copy) {
+      rho_copy[a] = d.x;
+      rho_copy[a + nx] = d.y;
+    }
+    sm[p * nx + brev(j, m.lx)] = d;
   }
   __syncthreads();
   smem_fft<true>(sm, m.lx, pairs, 1, nx, tw, false, false);

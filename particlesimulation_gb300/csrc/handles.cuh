@@ -22,7 +22,8 @@ int launch_deposit(int is, const float4* pm, int n, MeshDims m, float scale, u64
                    const int* stop, cudaStream_t st);
 int fft_configure(const MeshDims& m);
 int launch_poisson(u64* rho, float2* spec, float* phi, const float* ghat, const float2* tw,
-                   int nmax, MeshDims m, float fx_inv, const int* stop, cudaStream_t st);
+                   int nmax, MeshDims m, float fx_inv, const int* stop, cudaStream_t st,
+                   float* rho_copy = nullptr);
 int launch_green(float* ghat, MeshDims m, int gf, int is, int fds, double a, cudaStream_t st);
 int launch_interp(bool kdk, float4* pm, float4* vi, float4* acc, int n, const float* phi,
                   const StepParams& sp, float kick, int drift, int* stop, cudaStream_t st);
@@ -43,6 +44,7 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
 
 struct pmgb_p3m;
 struct pmgb_closure;
+struct pmgb_diag;
 
 struct pmgb_pm {
   pmgb_pm_config cfg{};
@@ -72,6 +74,7 @@ struct pmgb_pm {
   float stage_ms[5] = {0, 0, 0, 0, 0};
   float* stage = nullptr;      // 9 n floats: positions, velocities, accelerations (original order)
   float* mass_code = nullptr;  // n floats, code-unit masses in original order
+  pmgb_diag* diag = nullptr;   // run diagnostics (diag.cu), null when off
 };
 
 struct pmgb_p3m {
@@ -96,4 +99,16 @@ namespace pmgb {
 int closure_apply(pmgb_pm* h);
 // P3M handle over pm; attach = make it pm's pair pass (api.cu).
 int p3m_create_internal(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out, bool attach);
+
+// Run diagnostics (diag.cu).  diag_density: the float density buffer the Poisson solve fills
+// while diagnostics are on (else null).  diag_run_begin: the start of a run (records cleared,
+// expected momentum = current momentum).  diag_after_drift: one record of the state just
+// drifted by the iteration tagged `tag`; skipped on device if an earlier iteration escaped.
+// diag_before_drift: makes sure the density of the current positions is available for the
+// next record (advance() starts with a drift whose force may predate the diagnostics).
+float* diag_density(pmgb_pm* h);
+int diag_run_begin(pmgb_pm* h);
+int diag_before_drift(pmgb_pm* h);
+int diag_after_drift(pmgb_pm* h, int tag);
+void diag_free(pmgb_pm* h);
 }  // namespace pmgb

@@ -22,7 +22,7 @@ __global__ void __launch_bounds__(256) interp_kernel(float4* __restrict__ pm, fl
                                                      float4* __restrict__ acc, int n,
                                                      const float* __restrict__ phi, StepParams sp,
                                                      float kick, int drift, int* stop) {
-  if (*stop) return;
+  if (stopped_before(stop, KDK && drift, sp.step_tag)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   interp_particle<IS, FDS, KDK>(pm, vi, acc, i, phi, sp, kick, drift, stop);
@@ -58,7 +58,7 @@ int launch_interp(bool kdk, float4* pm, float4* vi, float4* acc, int n, const fl
 __global__ void kick_drift_kernel(float4* __restrict__ pm, float4* __restrict__ vi,
                                   const float4* __restrict__ acc, int n, StepParams sp, float kick,
                                   int drift, int* stop) {
-  if (*stop) return;
+  if (stopped_before(stop, drift != 0, sp.step_tag)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   float4 p = pm[i], v = vi[i];

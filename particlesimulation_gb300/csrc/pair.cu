@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(PAIR_THREADS) pair_kernel(
     StepParams sp, float kick, int drift, int kdk, float4* __restrict__ pm_out,
     float4* __restrict__ vi_out, float4* __restrict__ acc_out, unsigned long long* __restrict__ npairs,
     int* stop) {
-  if (*stop) return;
+  if (stopped_before(stop, kdk && drift, sp.step_tag)) return;
   // (T[t], T[t+1] - T[t]); entry 499 = (T[499], 0) so that t = 499 at the cutoff is in range
   __shared__ float2 tab[500];
   __shared__ float4 jbuf[PAIR_WARPS][32];

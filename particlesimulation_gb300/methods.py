@@ -132,11 +132,40 @@ class PMMethod:
     def pmMethodStep(self):
         check(lib().pmgb_pm_method_step(self._h))
 
-    def run(self, simLength: int):
-        """PMMethod::run without recorder: returns (escaped, steps_done)."""
+    def run(self, simLength: int, collectDiagnostics: bool = False):
+        """PMMethod::run without recorder: returns (escaped, steps_done).  collectDiagnostics
+        records the reference's per-iteration diagnostics (read them with ``diagnostics()``);
+        it turns them on with room for this run if they are off or too small."""
+        if collectDiagnostics:
+            self._ensure_diagnostics(int(simLength) + 1)
         done = C.c_int(0)
         rc = check(lib().pmgb_pm_run(self._h, int(simLength), C.byref(done)))
         return rc == _lib.PMGB_EESCAPED, done.value
+
+    # -- run diagnostics (SimInfo) --
+    def setDiagnostics(self, capacity: int):
+        """Record up to ``capacity`` diagnostics records during run / advance (0 = off)."""
+        check(lib().pmgb_pm_set_diagnostics(self._h, int(capacity)))
+        self._diag_cap = int(capacity)
+
+    def _ensure_diagnostics(self, capacity: int):
+        if getattr(self, "_diag_cap", 0) < capacity:
+            self.setDiagnostics(capacity)
+
+    def diagnostics(self):
+        """The records taken so far as a dict of float64 arrays (original units): potential_energy,
+        kinetic_energy, momentum (R, 3), angular_momentum (R, 3), expected_momentum (R, 3),
+        external_potential_energy; ``records`` is the raw (R, 12) array and ``taken`` the
+        number of records taken (more than R if some were dropped for lack of capacity)."""
+        cap = getattr(self, "_diag_cap", 0)
+        rec = np.zeros((max(cap, 1), _lib.DIAG_WIDTH), np.float64)
+        cnt = C.c_int(0)
+        check(lib().pmgb_pm_get_diagnostics(self._h, rec.ctypes.data_as(C.POINTER(C.c_double)),
+                                            cap, C.byref(cnt)))
+        rec = rec[: min(cnt.value, cap)].copy()
+        return dict(records=rec, taken=cnt.value, potential_energy=rec[:, 0],
+                    kinetic_energy=rec[:, 1], momentum=rec[:, 2:5], angular_momentum=rec[:, 5:8],
+                    expected_momentum=rec[:, 8:11], external_potential_energy=rec[:, 11])
 
     def advance(self, nSteps: int):
         """nSteps more iterations of run()'s loop body (drift, force, kick), continuing from the
@@ -247,7 +276,11 @@ class P3MMethod:
         """pmMethodStep + calculateShortRangeForces + correctAccelerations."""
         check(lib().pmgb_p3m_force(self._h))
 
-    def run(self, simLength: int):
+    def run(self, simLength: int, collectDiagnostics: bool = False):
+        """P3MMethod::run without recorder: returns (escaped, steps_done); diagnostics as
+        PMMethod.run (read them with ``pm.diagnostics()``)."""
+        if collectDiagnostics:
+            self.pm._ensure_diagnostics(int(simLength) + 1)
         done = C.c_int(0)
         rc = check(lib().pmgb_p3m_run(self._h, int(simLength), C.byref(done)))
         return rc == _lib.PMGB_EESCAPED, done.value

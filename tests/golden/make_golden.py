@@ -1,7 +1,8 @@
 """Generates tests/golden/*.npz from the reference's own CPU code (oracle/_ref/libpsref.so,
 compiled from the reference sources by oracle/Makefile).
 
-Run where the reference sources exist:  python tests/golden/make_golden.py
+Run where the reference sources exist:  python tests/golden/make_golden.py [diagnostics]
+(with "diagnostics", only diagnostics.npz is rewritten).
 Every case is a small seeded input; each fixture stores the inputs, the settings and the
 reference's outputs (float32), so tests on a machine without the reference still compare
 against the reference itself.
@@ -55,6 +56,38 @@ def pm_cases():
 
 
 MESH_CASES = ("pm_is1_fd0_gf0", "pm_is2_fd0_gf2", "pm_is2_fd1_gf1", "pm_is0_fd0_gf3")
+
+
+def diagnostics_fixture():
+    """Runs with collectDiagnostics = true: the reference's recorded energy, momentum, angular
+    momentum and expected momentum per iteration (StateRecorder text files), PM with an external
+    field, P3M, and a run that stops on an escaped particle."""
+    H = 30.0 / 16
+    p, v, m = inputs(60, 900, 8.0, 22.0)
+    cases = {}
+    cfg = O.PMConfig(grid=(32, 32, 32), box=(30.0, 30.0, 30.0), H=H, DT=0.1, G=1.0,
+                     interpolation=1, finite_diff=0, greens=0, diameter=0.0,
+                     ext=(15.0, 15.0, 15.0, 3.0, 0.5, 1.0))
+    x, vv, esc, d = O.ref_run(cfg, None, p, v, m, 5, diagnostics=True)
+    cases["pm_ext"] = dict(pos=p, vel=v, mass=m, diag=d, escaped=np.int32(esc),
+                           sim_length=np.int32(5), **_cfg_arrays(cfg))
+    cfg = O.PMConfig(grid=(32, 32, 32), box=(30.0, 30.0, 30.0), H=H, DT=0.1, G=1.0,
+                     interpolation=2, finite_diff=0, greens=2, diameter=3 * H)
+    q = O.P3MConfig(comp_box=(30.0, 30.0, 30.0), cutoff=3 * H, diameter=3 * H, cloud_shape=1)
+    x, vv, esc, d = O.ref_run(cfg, q, p, v, m, 3, diagnostics=True)
+    cases["p3m"] = dict(pos=p, vel=v, mass=m, diag=d, escaped=np.int32(esc),
+                        sim_length=np.int32(3), **_cfg_arrays(cfg), **_p3m_arrays(q))
+    pe = p.copy()
+    pe[:10, 0] = 29.6
+    ve = v.copy()
+    ve[:10, 0] = 0.05 * 30
+    cfg = O.PMConfig(grid=(32, 32, 32), box=(30.0, 30.0, 30.0), H=H, DT=0.1, G=1.0,
+                     interpolation=1, finite_diff=0, greens=0, diameter=0.0)
+    x, vv, esc, d = O.ref_run(cfg, None, pe, ve, m, 6, diagnostics=True)
+    cases["escape"] = dict(pos=pe, vel=ve, mass=m, diag=d, escaped=np.int32(esc),
+                           sim_length=np.int32(6), **_cfg_arrays(cfg))
+    np.savez_compressed(os.path.join(HERE, "diagnostics.npz"),
+                        **{f"{c}/{k}": a for c, dd in cases.items() for k, a in dd.items()})
 
 
 def main():
@@ -164,4 +197,8 @@ def _p3m_arrays(q):
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["diagnostics"]:
+        diagnostics_fixture()
+    else:
+        main()
+        diagnostics_fixture()

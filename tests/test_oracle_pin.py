@@ -140,3 +140,37 @@ def test_port_vs_live_reference_p3m_and_cells():
         b = O.ref_chaining_mesh(q, H, pc, ys)
         np.testing.assert_array_equal(a[0], b[0])
         np.testing.assert_array_equal(a[1], b[1])
+
+
+# ---------------------------------------------------------------- run diagnostics ---
+def _check_diag_vs_reference(rec, ref):
+    """Energies: the reference prints them with std::to_string (6 decimals) after summing in
+    float; vectors: printed with %.6e, summed in float over the particles."""
+    assert rec.shape == ref.shape
+    assert np.abs(rec[:, :2] - ref[:, :2]).max() < 1.5e-6
+    for sl in (slice(2, 5), slice(5, 8), slice(8, 11)):
+        scale = np.abs(ref[:, sl]).max()
+        assert np.abs(rec[:, sl] - ref[:, sl]).max() < 1e-5 * scale
+
+
+@pytest.mark.parametrize("case", ["pm_ext", "p3m", "escape"])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_port_diagnostics_match_golden(case, prec):
+    d = load_npz("diagnostics.npz")[case]
+    q = p3m_from(d) if "flags" in d else None
+    _, _, esc, rec = O.port_run(cfg_from(d), q, d["pos"], d["vel"], d["mass"],
+                                int(d["sim_length"]), prec=prec, diagnostics=True)
+    assert esc == bool(d["escaped"])
+    _check_diag_vs_reference(rec, d["diag"])
+
+
+@ref
+def test_port_diagnostics_vs_live_reference():
+    from particlesimulation_gb300 import workloads as W
+    w = W.plummer_cluster(n=3000, seed=9, grid=32)
+    cfg = O.PMConfig(grid=w.grid, box=w.box, H=w.H, DT=w.DT, G=w.G, interpolation=2,
+                     finite_diff=1, greens=1, diameter=3 * w.H, ext=(15.0, 14.0, 16.0, 4.0, 0.3, 1.0))
+    _, _, esc, ref_rec = O.ref_run(cfg, None, w.pos, w.vel, w.mass, 4, diagnostics=True)
+    _, _, esc2, rec = O.port_run(cfg, None, w.pos, w.vel, w.mass, 4, prec=0, diagnostics=True)
+    assert esc == esc2 and not esc
+    _check_diag_vs_reference(rec, ref_rec)
