@@ -255,13 +255,14 @@ def run_ours(args):
         t = statistics.median(pair_ms) * 1e-3
         achieved = flop / t / 1e12
         traffic = None  # dram read + write bytes of one launch, from the committed ncu summary
-        prof = os.path.join(ROOT, "profiles", f"pair_kernel_{w.name}.md")
+        prof = os.path.join(ROOT, "profiles", f"pair_slot_kernel_{w.name}.md")
         if os.path.exists(prof):
             with open(prof) as f:
                 for line in f:
                     if line.startswith("dram_bytes_per_launch:"):
                         traffic = float(line.split(":", 1)[1].split()[0])
-        roofline = {"kernel": "pair_kernel", "bound": "fp32", "achieved": round(achieved, 3),
+        roofline = {"kernel": "pair_slot_kernel + pair_epilogue_kernel", "bound": "fp32",
+                    "achieved": round(achieved, 3),
                     "peak": round(fp32_peak, 3), "unit": "TFLOP/s",
                     "frac": round(achieved / fp32_peak, 4), "traffic": traffic,
                     "peak_source": "FP32 FMA probe measured in this run (pmgb_fp32_peak_probe); "

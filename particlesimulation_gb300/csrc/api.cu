@@ -187,7 +187,7 @@ int force(pmgb_pm* h, int kdk, float kick, int drift, int tag, bool timed) {
                    q->item_cnt, q->item_off, q->nitems, q->items, q->counter, q->pp, q->table, sp,
                    kick, drift, kdk, h->pm[1 - h->cur], h->vi[1 - h->cur], h->acc,
                    q->count_pairs ? q->npairs : nullptr, stop,
-                   h->num_sms, timed ? h->ev[4] : nullptr, h->st);
+                   h->num_sms, timed ? h->ev[4] : nullptr, h->st, h->equal_mass, q->slots, n);
   if (rc) return rc;
   if (kdk) {
     h->cur = 1 - h->cur;
@@ -354,6 +354,7 @@ int pmgb_pm_create(const pmgb_pm_config* cfg, int n, const float* state, const f
   {
     std::vector<float> mc(N, 0.f);
     for (int i = 0; i < n; ++i) mc[i] = hp[i].w;
+    h->equal_mass = n > 0 && std::all_of(mc.begin(), mc.begin() + n, [&](float m) { return m == mc[0]; });
     if (cudaMemcpyAsync(h->mass_code, mc.data(), N * sizeof(float), cudaMemcpyHostToDevice, h->st) != cudaSuccess ||
         cudaStreamSynchronize(h->st) != cudaSuccess) {
       set_error("mass upload failed");
@@ -596,8 +597,11 @@ int p3m_create_internal(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out,
   int rc;
   if ((rc = dalloc(&q->cell_start, ntot + 1)) || (rc = dalloc(&q->item_cnt, ntot)) ||
       (rc = dalloc(&q->item_off, ntot)) || (rc = dalloc(&q->nitems, 1)) || (rc = dalloc(&q->counter, 1)) ||
-      (rc = dalloc(&q->items, (size_t)pm->n + ntot + 32)) || (rc = dalloc(&q->table, 500)) ||
-      (rc = dalloc(&q->npairs, 1))) {
+      // work items: 32-particle slices (pair counting, direct formula) or 64-particle slices x 27
+      // neighbours (the table pass), and its 27 partial-force slots per particle
+      (rc = dalloc(&q->items, 27 * ((size_t)pm->n / 64 + ntot) + (size_t)pm->n + 32)) ||
+      (rc = dalloc(&q->table, 500)) || (rc = dalloc(&q->npairs, 1)) ||
+      (rc = dalloc(&q->slots, 27 * (size_t)std::max(pm->n, 1)))) {
     pmgb_p3m_destroy(q);
     return rc;
   }
@@ -622,7 +626,8 @@ int pmgb_p3m_destroy(pmgb_p3m* q) {
     if (q->pm->p3m == q) q->pm->p3m = nullptr;
     q->pm->since_sort = 1 << 30;
   }
-  void* ptrs[] = {q->cell_start, q->item_cnt, q->item_off, q->nitems, q->counter, q->items, q->table, q->npairs};
+  void* ptrs[] = {q->cell_start, q->item_cnt, q->item_off, q->nitems, q->counter, q->items, q->table, q->npairs,
+                  q->slots};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete q;

@@ -38,7 +38,7 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
                 u32* counter, const PairParams& pp, const float* table, const StepParams& sp,
                 float kick, int drift, int kdk, float4* pm_out, float4* vi_out, float4* acc_out,
                 unsigned long long* npairs, int* stop, int num_sms, cudaEvent_t ev_pair,
-                cudaStream_t st);
+                cudaStream_t st, int equal_mass, float4* slots, int n);
 
 }  // namespace pmgb
 
@@ -75,6 +75,7 @@ struct pmgb_pm {
   float* stage = nullptr;      // 9 n floats: positions, velocities, accelerations (original order)
   float* mass_code = nullptr;  // n floats, code-unit masses in original order
   pmgb_diag* diag = nullptr;   // run diagnostics (diag.cu), null when off
+  int equal_mass = 0;          // every particle has the same mass (pair pass folds it)
 };
 
 struct pmgb_p3m {
@@ -91,6 +92,7 @@ struct pmgb_p3m {
   pmgb::PairParams pp{};
   unsigned long long* npairs = nullptr;
   int count_pairs = 0;  // count in-range pairs during force evaluations (pmgb_p3m_set_pair_counting)
+  float4* slots = nullptr;  // 27 x n partial short-range accelerations (pair.cu, table pass)
 };
 
 namespace pmgb {

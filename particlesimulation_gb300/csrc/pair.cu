@@ -10,6 +10,9 @@
 // GPU formulation.  The reference walks 13 half-shell neighbour cells and scatters -F_ij into
 // per-neighbour slots of j.  Here each particle gathers from all 27 cells (each pair is
 // evaluated twice, once per side), so no scatter, no atomics and a deterministic result.
+// Two kernels: pair_slot_kernel (below; the table pass of every run, finer work items and
+// fewer instructions per pair) and pair_kernel, described here, which also counts pairs and
+// evaluates the table-free formula.
 // Work items are 32-particle slices of one cell (the cells are y-sorted, so a slice spans a
 // narrow y range); a warp takes items from a global counter (dense cells cost more, the counter
 // balances).  For each neighbour cell a lane binary-searches the y window
@@ -201,24 +204,221 @@ __global__ void __launch_bounds__(PAIR_THREADS) pair_kernel(
   }
 }
 
+// ------------------------------------------------------- table pair pass, slotted ----
+// The table path without pair counting.  Work is split finer than one item per slice so that
+// the dense cells of clustered inputs do not leave a long tail: a work item is one 64-particle
+// slice of a cell against ONE of its 27 neighbour cells, and it writes the slice's partial
+// short-range acceleration from that neighbour into slot k of each particle
+// (slots[k * n + i], k = 0..26, zero for a neighbour outside the mesh).  An epilogue kernel adds
+// the 27 slots in a fixed order (so the result is deterministic), the PM acceleration, and in a
+// run the kick and drift.  Fewer instructions per candidate pair than pair_kernel:
+//  * each lane holds two i particles, so every staged candidate is read once from shared
+//    memory for two pairs;
+//  * the table is kept in intercept form per segment, f(xi) = A[t] + xi S[t] with
+//    S[t] = T[t+1] - T[t] (float, as the reference forms it) and A[t] = T[t] - t S[t] (double,
+//    rounded once): one FMA instead of forming xi - t;
+//  * t = floor(xi) is one round-down add of 1.5 * 2^23 (FADD.RM) and an integer subtract;
+//  * the cutoff test is folded into the table: segments t >= 499 (xi >= 499, i.e.
+//    r^2 >= re^2) are zero, and xi is clamped to 499.5 so t never leaves the table;
+//  * with equal masses (every benchmark workload) the mass is folded into the table.
+// The y window of the slice in the neighbour's y-sorted list is found by a warp-cooperative
+// search (32 probes per round).  Per-chunk partial sums are added with Kahan compensation.
+constexpr int SLOT_IPL = 2;                  // i particles per lane
+constexpr int SLOT_SLICE = 32 * SLOT_IPL;    // particles per work item
+constexpr int SLOT_TAB = 500;                // segments 0..499 (499 = zero)
+constexpr int NNB = 27;                      // neighbour cells (and slots) per particle
+
+struct SlotI {
+  float4 p;
+  float sx, sy, sz, cx, cy, cz;
+  float px, py, pz;
+};
+
+template <bool EQM>
+__device__ __forceinline__ void slot_pair(SlotI& I, const float4& q, float inv_d2,
+                                          const float2* __restrict__ tab) {
+  const float dx = I.p.x - q.x, dy = I.p.y - q.y, dz = I.p.z - q.z;
+  const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+  const float xi = fminf(r2 * inv_d2, 499.5f);
+  const float tf = __fadd_rd(xi, kMagic);  // kMagic + floor(xi)
+  const int t = __float_as_int(tf) - __float_as_int(kMagic);
+  const float2 ab = tab[t];
+  float f = fmaf(xi, ab.y, ab.x);
+  if (!EQM) f *= q.w;
+  I.px = fmaf(f, dx, I.px);
+  I.py = fmaf(f, dy, I.py);
+  I.pz = fmaf(f, dz, I.pz);
+}
+
+// First index in [lo, hi) whose y is >= v (UPPER = false) or > v (UPPER = true), found by the
+// whole warp: each round probes 32 evenly spaced entries and keeps the one gap that holds the
+// boundary, so a list of n entries takes about log32(n) rounds of loads.
+template <bool UPPER>
+__device__ __forceinline__ int warp_y_bound(const float4* __restrict__ pm, int lo, int hi, float v,
+                                            int lane) {
+  while (hi - lo > 32) {
+    const int step = (hi - lo + 31) >> 5;
+    const int idx = lo + lane * step;
+    bool below = false;
+    if (idx < hi) {
+      const float y = __ldg(&pm[idx].y);
+      below = UPPER ? (y <= v) : (y < v);
+    }
+    const int c = __popc(__ballot_sync(0xFFFFFFFFu, below));
+    const int nlo = c > 0 ? lo + (c - 1) * step + 1 : lo;
+    hi = min(hi, lo + c * step);
+    lo = nlo;
+  }
+  const int idx = lo + lane;
+  bool below = false;
+  if (idx < hi) {
+    const float y = __ldg(&pm[idx].y);
+    below = UPPER ? (y <= v) : (y < v);
+  }
+  return lo + __popc(__ballot_sync(0xFFFFFFFFu, below));
+}
+
+template <bool EQM>
+__global__ void __launch_bounds__(PAIR_THREADS) pair_slot_kernel(
+    const float4* __restrict__ pm, int n, const int* __restrict__ cell_start,
+    const int2* __restrict__ items, const u32* __restrict__ nitems_p, u32* __restrict__ counter,
+    ChainDimsP cd, PairParams pp, const float* __restrict__ table, float4* __restrict__ slots,
+    const int* __restrict__ stop) {
+  if (*stop) return;
+  __shared__ float2 tab[SLOT_TAB];
+  __shared__ float4 jbuf[PAIR_WARPS][32];
+  {
+    // every particle has the same mass when EQM: fold it into the table
+    const double mj = EQM ? (double)__ldg(&pm[0].w) : 1.0;
+    for (int t = threadIdx.x; t < SLOT_TAB; t += PAIR_THREADS) {
+      float2 ab = make_float2(0.f, 0.f);
+      if (t < 499) {
+        const float a = table[t];
+        const float s = table[t + 1] - a;
+        const double A = (double)a - (double)t * (double)s;
+        ab = make_float2((float)(A * mj), (float)((double)s * mj));
+      }
+      tab[t] = ab;
+    }
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const u32 nitems = *nitems_p;
+  const float inv_d2 = pp.inv_d2;
+  for (;;) {
+    u32 it = 0;
+    if (lane == 0) it = atomicAdd(counter, 1u);
+    it = __shfl_sync(0xFFFFFFFFu, it, 0);
+    if (it >= nitems) break;
+    const int2 item = items[it];
+    const int cell = item.x / NNB;
+    const int k = item.x - cell * NNB;
+    const int cend = cell_start[cell + 1];
+    const int last = min(item.y + SLOT_SLICE - 1, cend - 1);
+    SlotI I[SLOT_IPL];
+#pragma unroll
+    for (int u = 0; u < SLOT_IPL; ++u) {
+      const int i = item.y + 32 * u + lane;
+      I[u].p = pm[i < cend ? i : last];
+      I[u].sx = I[u].sy = I[u].sz = I[u].cx = I[u].cy = I[u].cz = 0.f;
+    }
+    if (cell < cd.ncells) {
+      const int gx = cell % cd.Mx, gy = (cell / cd.Mx) % cd.My, gz = cell / (cd.Mx * cd.My);
+      const int nx = gx + k % 3 - 1, ny = gy + (k / 3) % 3 - 1, nz = gz + k / 9 - 1;
+      if (nx >= 0 && ny >= 0 && nz >= 0 && nx < cd.Mx && ny < cd.My && nz < cd.Mz) {
+        const int cn = nx + ny * cd.Mx + nz * cd.Mx * cd.My;
+        int b = cell_start[cn];
+        int e = cell_start[cn + 1];
+        if (pp.ysort && e > b) {
+          // y range of the slice: its first particle (lane 0, u = 0) and its last one
+          const float ylo = __shfl_sync(0xFFFFFFFFu, I[0].p.y, 0) - pp.re;
+          const float yhi = __ldg(&pm[last].y) + pp.re;
+          b = warp_y_bound<false>(pm, b, e, ylo, lane);
+          e = warp_y_bound<true>(pm, b, e, yhi, lane);
+        }
+        for (int j0 = b; j0 < e; j0 += 32) {
+          const int jj = j0 + lane;
+          jbuf[warp][lane] = jj < e ? pm[jj] : make_float4(3.0e30f, 3.0e30f, 3.0e30f, 0.f);
+          __syncwarp();
+          const int cnt = min(32, e - j0);
+#pragma unroll
+          for (int u = 0; u < SLOT_IPL; ++u) I[u].px = I[u].py = I[u].pz = 0.f;
+#pragma unroll 4
+          for (int s = 0; s < cnt; ++s) {
+            const float4 q = jbuf[warp][s];
+#pragma unroll
+            for (int u = 0; u < SLOT_IPL; ++u) slot_pair<EQM>(I[u], q, inv_d2, tab);
+          }
+          __syncwarp();
+#pragma unroll
+          for (int u = 0; u < SLOT_IPL; ++u) {
+            kahan_add(I[u].sx, I[u].cx, I[u].px);
+            kahan_add(I[u].sy, I[u].cy, I[u].py);
+            kahan_add(I[u].sz, I[u].cz, I[u].pz);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < SLOT_IPL; ++u) {
+      const int i = item.y + 32 * u + lane;
+      if (i < cend) slots[(size_t)k * n + i] = make_float4(I[u].sx, I[u].sy, I[u].sz, 0.f);
+    }
+  }
+}
+
+// Sum of the 27 slots in slot order (Kahan), plus the PM acceleration; in a run the kick, the
+// drift, the unit round trip and the escape test, writing the new state to the other buffers.
+__global__ void __launch_bounds__(256) pair_epilogue_kernel(
+    const float4* __restrict__ pm, const float4* __restrict__ vi, const float4* __restrict__ acc_pm,
+    const float4* __restrict__ slots, int n, StepParams sp, float kick, int drift, int kdk,
+    float4* __restrict__ pm_out, float4* __restrict__ vi_out, float4* __restrict__ acc_out,
+    int* stop) {
+  if (stopped_before(stop, kdk && drift, sp.step_tag)) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+#pragma unroll 9
+  for (int k = 0; k < NNB; ++k) {
+    const float4 v = slots[(size_t)k * n + i];
+    kahan_add(sx, cx, v.x);
+    kahan_add(sy, cy, v.y);
+    kahan_add(sz, cz, v.z);
+  }
+  const float4 ap = acc_pm[i];
+  const float3 a = make_float3(ap.x + sx, ap.y + sy, ap.z + sz);
+  if (kdk) {
+    float4 p = pm[i], v = vi[i];
+    kick_drift(sp, p, v, a, kick, drift, stop);
+    pm_out[i] = p;
+    vi_out[i] = v;
+  }
+  acc_out[i] = make_float4(a.x, a.y, a.z, 0.f);
+}
+
 // ------------------------------------------------------------------ work items ---------
+// per_slice = 1: one item (cell, slice start) per 32-particle slice; per_slice = 27: items
+// (cell * 27 + k, slice start) per 64-particle slice and neighbour k.
 __global__ void item_count_kernel(const int* __restrict__ cell_start, int ncells_total,
-                                  u32* __restrict__ cnt, const int* stop) {
+                                  u32* __restrict__ cnt, int slice, int per_slice, const int* stop) {
   if (*stop) return;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells_total) return;
   const int n = cell_start[c + 1] - cell_start[c];
-  cnt[c] = (u32)((n + 31) / 32);
+  cnt[c] = (u32)((n + slice - 1) / slice) * (u32)per_slice;
 }
 
 __global__ void item_build_kernel(const int* __restrict__ cell_start, const u32* __restrict__ off,
-                                  int ncells_total, int2* __restrict__ items, const int* stop) {
+                                  int ncells_total, int2* __restrict__ items, int slice,
+                                  int per_slice, const int* stop) {
   if (*stop) return;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells_total) return;
   const int b = cell_start[c], e = cell_start[c + 1];
   u32 o = off[c];
-  for (int s = b; s < e; s += 32) items[o++] = make_int2(c, s);
+  for (int s = b; s < e; s += slice)
+    for (int k = 0; k < per_slice; ++k) items[o++] = make_int2(c * per_slice + k, s);
 }
 
 int exclusive_scan(const u32* in, u32* out, int n, u32* total, cudaStream_t st);
@@ -228,13 +428,17 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
                 u32* counter, const PairParams& pp, const float* table, const StepParams& sp,
                 float kick, int drift, int kdk, float4* pm_out, float4* vi_out, float4* acc_out,
                 unsigned long long* npairs, int* stop, int num_sms, cudaEvent_t ev_pair,
-                cudaStream_t st) {
+                cudaStream_t st, int equal_mass, float4* slots, int n) {
   const int ncells = Mx * My * Mz;
   const int ntot = ncells + 1;  // + the bucket of particles outside the chaining mesh
-  item_count_kernel<<<(ntot + 255) / 256, 256, 0, st>>>(cell_start, ntot, item_cnt, stop);
+  const bool slotted = pp.use_table && !npairs && slots;
+  const int slice = slotted ? SLOT_SLICE : 32;
+  const int per_slice = slotted ? NNB : 1;
+  item_count_kernel<<<(ntot + 255) / 256, 256, 0, st>>>(cell_start, ntot, item_cnt, slice, per_slice, stop);
   int rc = exclusive_scan(item_cnt, item_off, ntot, nitems, st);
   if (rc) return rc;
-  item_build_kernel<<<(ntot + 255) / 256, 256, 0, st>>>(cell_start, item_off, ntot, items, stop);
+  item_build_kernel<<<(ntot + 255) / 256, 256, 0, st>>>(cell_start, item_off, ntot, items, slice,
+                                                        per_slice, stop);
   PMGB_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(u32), st));
   if (npairs) PMGB_CUDA_TRY(cudaMemsetAsync(npairs, 0, sizeof(unsigned long long), st));
   if (ev_pair) PMGB_CUDA_TRY(cudaEventRecord(ev_pair, st));
@@ -242,7 +446,19 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
   const dim3 grid(num_sms * 8), block(PAIR_THREADS);
 #define PMGB_PAIR_ARGS pm, vi, acc_pm, cell_start, items, nitems, counter, cd, pp, table, sp, kick, \
                        drift, kdk, pm_out, vi_out, acc_out, npairs, stop
-  if (pp.use_table) {
+  int launches = 3;  // item count, item build, pair pass (the scan counts itself)
+  if (slotted) {
+    if (equal_mass)
+      pair_slot_kernel<true><<<grid, block, 0, st>>>(pm, n, cell_start, items, nitems, counter, cd, pp,
+                                                     table, slots, stop);
+    else
+      pair_slot_kernel<false><<<grid, block, 0, st>>>(pm, n, cell_start, items, nitems, counter, cd, pp,
+                                                      table, slots, stop);
+    if (n > 0)
+      pair_epilogue_kernel<<<(n + 255) / 256, 256, 0, st>>>(pm, vi, acc_pm, slots, n, sp, kick, drift,
+                                                            kdk, pm_out, vi_out, acc_out, stop);
+    ++launches;
+  } else if (pp.use_table) {
     if (npairs) pair_kernel<true, true><<<grid, block, 0, st>>>(PMGB_PAIR_ARGS);
     else pair_kernel<true, false><<<grid, block, 0, st>>>(PMGB_PAIR_ARGS);
   } else {
@@ -251,7 +467,7 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
   }
 #undef PMGB_PAIR_ARGS
   PMGB_LAUNCH_CHECK();
-  count_launches(3);  // item count, item build, pair pass (the scan counts itself)
+  count_launches(launches);
   return PMGB_OK;
 }
 
