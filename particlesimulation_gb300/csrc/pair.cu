@@ -220,13 +220,21 @@ __global__ void __launch_bounds__(PAIR_THREADS) pair_kernel(
 //  * t = floor(xi) is one round-down add of 1.5 * 2^23 (FADD.RM) and an integer subtract;
 //  * the cutoff test is folded into the table: segments t >= 499 (xi >= 499, i.e.
 //    r^2 >= re^2) are zero, and xi is clamped to 499.5 so t never leaves the table;
-//  * with equal masses (every benchmark workload) the mass is folded into the table.
+//  * with equal masses (every benchmark workload) the mass is folded into the table;
+//  * the table is replicated 16 times, copy (lane mod 16) for each lane, so the per-lane lookups
+//    of a half warp fall into 16 distinct bank pairs whatever their segments (an 8-byte load
+//    of a warp then takes the minimum of two shared-memory wavefronts instead of about four);
+//    64 KB of shared memory, hence 512-thread CTAs to keep 32 warps per SM.
 // The y window of the slice in the neighbour's y-sorted list is found by a warp-cooperative
 // search (32 probes per round).  Per-chunk partial sums are added with Kahan compensation.
 constexpr int SLOT_IPL = 2;                  // i particles per lane
 constexpr int SLOT_SLICE = 32 * SLOT_IPL;    // particles per work item
 constexpr int SLOT_TAB = 500;                // segments 0..499 (499 = zero)
+constexpr int SLOT_REP = 16;                 // table copies (lane mod 16)
 constexpr int NNB = 27;                      // neighbour cells (and slots) per particle
+constexpr int SLOT_THREADS = 512;
+constexpr int SLOT_WARPS = SLOT_THREADS / 32;
+constexpr int SLOT_SMEM = SLOT_TAB * SLOT_REP * 8 + SLOT_WARPS * 32 * 16;  // table + staging
 
 struct SlotI {
   float4 p;
@@ -242,7 +250,7 @@ __device__ __forceinline__ void slot_pair(SlotI& I, const float4& q, float inv_d
   const float xi = fminf(r2 * inv_d2, 499.5f);
   const float tf = __fadd_rd(xi, kMagic);  // kMagic + floor(xi)
   const int t = __float_as_int(tf) - __float_as_int(kMagic);
-  const float2 ab = tab[t];
+  const float2 ab = tab[t * SLOT_REP];  // tab already points at this lane's copy
   float f = fmaf(xi, ab.y, ab.x);
   if (!EQM) f *= q.w;
   I.px = fmaf(f, dx, I.px);
@@ -279,18 +287,19 @@ __device__ __forceinline__ int warp_y_bound(const float4* __restrict__ pm, int l
 }
 
 template <bool EQM>
-__global__ void __launch_bounds__(PAIR_THREADS) pair_slot_kernel(
+__global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
     const float4* __restrict__ pm, int n, const int* __restrict__ cell_start,
     const int2* __restrict__ items, const u32* __restrict__ nitems_p, u32* __restrict__ counter,
     ChainDimsP cd, PairParams pp, const float* __restrict__ table, float4* __restrict__ slots,
     const int* __restrict__ stop) {
   if (*stop) return;
-  __shared__ float2 tab[SLOT_TAB];
-  __shared__ float4 jbuf[PAIR_WARPS][32];
+  extern __shared__ float4 slot_smem[];
+  float4 (*jbuf)[32] = reinterpret_cast<float4 (*)[32]>(slot_smem);
+  float2* tab_all = reinterpret_cast<float2*>(slot_smem + SLOT_WARPS * 32);
   {
     // every particle has the same mass when EQM: fold it into the table
     const double mj = EQM ? (double)__ldg(&pm[0].w) : 1.0;
-    for (int t = threadIdx.x; t < SLOT_TAB; t += PAIR_THREADS) {
+    for (int t = threadIdx.x; t < SLOT_TAB; t += SLOT_THREADS) {
       float2 ab = make_float2(0.f, 0.f);
       if (t < 499) {
         const float a = table[t];
@@ -298,12 +307,14 @@ __global__ void __launch_bounds__(PAIR_THREADS) pair_slot_kernel(
         const double A = (double)a - (double)t * (double)s;
         ab = make_float2((float)(A * mj), (float)((double)s * mj));
       }
-      tab[t] = ab;
+#pragma unroll
+      for (int c = 0; c < SLOT_REP; ++c) tab_all[t * SLOT_REP + c] = ab;
     }
   }
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
+  const float2* tab = tab_all + (lane & (SLOT_REP - 1));
   const u32 nitems = *nitems_p;
   const float inv_d2 = pp.inv_d2;
   for (;;) {
@@ -444,16 +455,20 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
   if (ev_pair) PMGB_CUDA_TRY(cudaEventRecord(ev_pair, st));
   ChainDimsP cd{Mx, My, Mz, ncells};
   const dim3 grid(num_sms * 8), block(PAIR_THREADS);
+  if (slotted) {  // 64 KB + staging of dynamic shared memory (set for the current device)
+    PMGB_CUDA_TRY(cudaFuncSetAttribute(pair_slot_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SLOT_SMEM));
+    PMGB_CUDA_TRY(cudaFuncSetAttribute(pair_slot_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SLOT_SMEM));
+  }
 #define PMGB_PAIR_ARGS pm, vi, acc_pm, cell_start, items, nitems, counter, cd, pp, table, sp, kick, \
                        drift, kdk, pm_out, vi_out, acc_out, npairs, stop
   int launches = 3;  // item count, item build, pair pass (the scan counts itself)
   if (slotted) {
     if (equal_mass)
-      pair_slot_kernel<true><<<grid, block, 0, st>>>(pm, n, cell_start, items, nitems, counter, cd, pp,
-                                                     table, slots, stop);
+      pair_slot_kernel<true><<<num_sms * 2, SLOT_THREADS, SLOT_SMEM, st>>>(
+          pm, n, cell_start, items, nitems, counter, cd, pp, table, slots, stop);
     else
-      pair_slot_kernel<false><<<grid, block, 0, st>>>(pm, n, cell_start, items, nitems, counter, cd, pp,
-                                                      table, slots, stop);
+      pair_slot_kernel<false><<<num_sms * 2, SLOT_THREADS, SLOT_SMEM, st>>>(
+          pm, n, cell_start, items, nitems, counter, cd, pp, table, slots, stop);
     if (n > 0)
       pair_epilogue_kernel<<<(n + 255) / 256, 256, 0, st>>>(pm, vi, acc_pm, slots, n, sp, kick, drift,
                                                             kdk, pm_out, vi_out, acc_out, stop);
