@@ -324,7 +324,7 @@ int set_pairs(pmgb_ensemble* e, int mult) {
     if (mult == 0) p = std::max(1, p / 2);
     if (mult == 2) p = (int)std::min<long long>(rowpairs, 2ll * p);
     q.pairs = p;
-    smem = std::max(smem, (size_t)(p * q.sp.m.nx + q.sp.m.nx / 2) * sizeof(float2));
+    smem = std::max(smem, (size_t)x_smem_elems(q.sp.m.nx, p) * sizeof(float2));
   }
   e->pair_mult = mult;
   e->x_smem = smem;
@@ -557,8 +557,7 @@ int pmgb_ensemble_create(int n_systems, const pmgb_pm_config* cfgs, const int* c
   }
   size_t col_smem = 0;
   for (auto& q : e->hsys)
-    col_smem = std::max(col_smem, (size_t)(std::max(q.sp.m.ny, q.sp.m.nz) * COL_TX +
-                                           std::max(q.sp.m.ny, q.sp.m.nz) / 2) * sizeof(float2));
+    col_smem = std::max(col_smem, (size_t)col_smem_elems(std::max(q.sp.m.ny, q.sp.m.nz)) * sizeof(float2));
   e->col_smem = col_smem;
   if (col_smem > 48 * 1024 &&
       cudaFuncSetAttribute(ens_fft_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)col_smem) != cudaSuccess)

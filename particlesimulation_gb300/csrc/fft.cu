@@ -15,9 +15,11 @@
 //   fft_cols(z) along z: forward, * G, inverse in the same shared-memory tile
 //   fft_cols(y) inverse
 //   fft_x_c2r   two rows per complex FFT, writes the potential (1/N is folded into G)
-// Inside a CTA the transforms are radix-2 in shared memory: decimation in time on bit-reversed
-// input for forward transforms, decimation in frequency (bit-reversed output) for inverse
-// ones, with twiddles computed in double on the host.
+// Inside a CTA the transforms run in shared memory in steps of up to 4 bits (radix 16, the 16
+// points of a butterfly group in registers, fft_body.cuh): decimation in time on bit-reversed
+// input for forward transforms, decimation in frequency (bit-reversed output) for inverse ones,
+// with twiddles computed in double on the host.  Each thread issues its global loads in
+// batches of 8 before using them, so a CTA keeps enough loads in flight to stream from HBM.
 #include "fft_body.cuh"
 
 namespace pmgb {
@@ -61,9 +63,9 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_cols_kernel(float2* __restric
 static int x_pairs(const MeshDims& m) { return x_pairs_default(m); }
 
 int fft_smem_bytes_max(const MeshDims& m) {
-  int a = (x_pairs(m) * m.nx + m.nx / 2) * (int)sizeof(float2);
-  int ny = (m.ny * COL_TX + m.ny / 2) * (int)sizeof(float2);
-  int nz = (m.nz * COL_TX + m.nz / 2) * (int)sizeof(float2);
+  int a = x_smem_elems(m.nx, x_pairs(m)) * (int)sizeof(float2);
+  int ny = col_smem_elems(m.ny) * (int)sizeof(float2);
+  int nz = col_smem_elems(m.nz) * (int)sizeof(float2);
   return a > ny ? (a > nz ? a : nz) : (ny > nz ? ny : nz);
 }
 
@@ -83,10 +85,10 @@ int launch_poisson(u64* rho, float2* spec, float* phi, const float* ghat, const 
                    float* rho_copy) {
   const int pairs = x_pairs(m);
   const int xblocks = (int)((long long)m.ny * m.nz / 2 / pairs);
-  const int xsmem = (pairs * m.nx + m.nx / 2) * (int)sizeof(float2);
+  const int xsmem = x_smem_elems(m.nx, pairs) * (int)sizeof(float2);
   const int ctiles = (m.nxp + COL_TX - 1) / COL_TX;
-  const int ysmem = (m.ny * COL_TX + m.ny / 2) * (int)sizeof(float2);
-  const int zsmem = (m.nz * COL_TX + m.nz / 2) * (int)sizeof(float2);
+  const int ysmem = col_smem_elems(m.ny) * (int)sizeof(float2);
+  const int zsmem = col_smem_elems(m.nz) * (int)sizeof(float2);
   fft_x_r2c_kernel<<<xblocks, FFT_THREADS, xsmem, st>>>(rho, spec, m, pairs, fx_inv, tw, nmax, stop, rho_copy);
   fft_cols_kernel<<<dim3(ctiles, m.nz), FFT_THREADS, ysmem, st>>>(spec, m, 1, 0, nullptr, tw, nmax, stop);
   fft_cols_kernel<<<dim3(ctiles, m.ny), FFT_THREADS, zsmem, st>>>(spec, m, 2, 2, ghat, tw, nmax, stop);
