@@ -187,6 +187,36 @@ int pmgb_pm_set_diagnostics(pmgb_pm* pm, int capacity);
  * (records beyond the capacity are dropped).  *count = 0 when diagnostics are off. */
 int pmgb_pm_get_diagnostics(pmgb_pm* pm, double* records, int max_records, int* count);
 
+/* ---------------------------------------------------------------- StateRecorder ------ */
+
+/* StateRecorder(particlesCnt, framesCnt, outputDirPath, positionsFile, energyFile,
+ * momentumFile, expectedMomentumFile, angularMomentumFile, fieldFile)
+ * (source/stateRecorder.cpp:5-44): creates output_dir, writes the int32 (n, frames) headers
+ * of the binary files.  names = the six file names in that order (positions, energy, momentum,
+ * expected momentum, angular momentum, field); NULL = the reference's defaults, an empty name
+ * = that output left out.  with_field reserves device room for field frames.  Frames are
+ * packed on the device and written by a host thread from pinned buffers as they fill. */
+typedef struct pmgb_recorder pmgb_recorder;
+int pmgb_recorder_create(int n, int frames, const char* output_dir, const char* const* names,
+                         int with_field, pmgb_recorder** out);
+int pmgb_recorder_destroy(pmgb_recorder* rec);
+
+/* StateRecorder::flush (source/stateRecorder.cpp:109-119): waits for the frames in flight,
+ * writes the text files; copies the output directory into dir_out (may be NULL). */
+int pmgb_recorder_flush(pmgb_recorder* rec, char* dir_out, int cap);
+
+/* Frames written to the binary files so far (after waiting for those in flight). */
+int pmgb_recorder_frames_written(pmgb_recorder* rec, long long* frames);
+
+/* PMMethod::run(stateRecorder, simLength, collectDiagnostics, recordField) and
+ * P3MMethod::run (source/pmMethod.cpp:62-135, source/p3mMethod.cpp:59-166): the run of
+ * pmgb_pm_run recording every iteration's positions (recordPositions), with record_field the
+ * acceleration of the iteration (recordField), with collect_diagnostics the energy and momentum
+ * lines (run diagnostics turned on with room for the run if needed); flushes the recorder at the
+ * end.  Returns like pmgb_pm_run. */
+int pmgb_pm_run_recorded(pmgb_pm* pm, pmgb_recorder* rec, int sim_length, int collect_diagnostics,
+                         int record_field, int* steps_done);
+
 /* ---------------------------------------------------------------- P3M --------------- */
 
 /* P3MMethod::P3MMethod (source/p3mMethod.cpp:19-48): chaining mesh and short-range force

@@ -49,6 +49,37 @@ struct DiagnosticsRecord {
 };
 static_assert(sizeof(DiagnosticsRecord) == PMGB_DIAG_WIDTH * sizeof(double), "record layout");
 
+// StateRecorder with the reference's constructor (include/stateRecorder.h:10-21); the files
+// and their formats are the reference's.  maxRecords (the reference's write-batch size) has no
+// counterpart: frames are written from device buffers as they fill.
+class StateRecorder {
+ public:
+  StateRecorder(int particlesCnt, int framesCnt, const std::string& outputDirPath,
+                const char* positionsFile = "positions.dat", const char* energyFile = "energy.txt",
+                const char* momentumFile = "momentum.txt",
+                const char* expectedMomentumFile = "expected_momentum.txt",
+                const char* angularMomentumFile = "angular_momentum.txt",
+                const char* fieldFile = "field.dat", int /*maxRecords*/ = 500) {
+    const char* names[6] = {positionsFile, energyFile, momentumFile, expectedMomentumFile,
+                            angularMomentumFile, fieldFile};
+    int rc = pmgb_recorder_create(particlesCnt, framesCnt, outputDirPath.c_str(), names, 1, &h);
+    if (rc != PMGB_OK) throw std::invalid_argument(pmgb_last_error());
+  }
+  ~StateRecorder() { pmgb_recorder_destroy(h); }
+  StateRecorder(const StateRecorder&) = delete;
+  StateRecorder& operator=(const StateRecorder&) = delete;
+
+  std::string flush() {
+    char buf[4096];
+    if (pmgb_recorder_flush(h, buf, sizeof buf) != PMGB_OK) throw std::runtime_error(pmgb_last_error());
+    return buf;
+  }
+  pmgb_recorder* handle() { return h; }
+
+ private:
+  pmgb_recorder* h = nullptr;
+};
+
 struct Particle {
   Vec3 position, velocity, acceleration;
   float mass{};
@@ -130,6 +161,20 @@ class PMMethodGPU {
     if (rc == PMGB_EESCAPED) std::cout << "Particle moved outside the computational box.\n";
     copyParticlesDeviceToHost();
     return std::string();
+  }
+
+  // PMMethod::run(stateRecorder, simLength, collectDiagnostics, recordField)
+  // (source/pmMethod.cpp:62-135): the reference's output files; returns the output directory.
+  std::string run(StateRecorder& stateRecorder, const int simLength, bool collectDiagnostics = false,
+                  bool recordField = false) {
+    if (collectDiagnostics) ensureDiagnostics(simLength + 1);
+    int done = 0;
+    int rc = pmgb_pm_run_recorded(h, stateRecorder.handle(), simLength, collectDiagnostics ? 1 : 0,
+                                  recordField ? 1 : 0, &done);
+    check(rc);
+    if (rc == PMGB_EESCAPED) std::cout << "Particle moved outside the computational box.\n";
+    copyParticlesDeviceToHost();
+    return stateRecorder.flush();
   }
 
   void pmMethodStep() { check(pmgb_pm_method_step(h)); }
@@ -246,6 +291,13 @@ class P3MMethod {
     check(rc);
     if (rc == PMGB_EESCAPED) std::cout << "Particle moved outside the computational box.\n";
     pm.copyParticlesDeviceToHost();
+  }
+
+  // P3MMethod::run(stateRecorder, simLength, collectDiagnostics, recordField)
+  // (source/p3mMethod.cpp:59-166).
+  std::string run(StateRecorder& stateRecorder, const int simLength, bool collectDiagnostics = false,
+                  bool recordField = false) {
+    return pm.run(stateRecorder, simLength, collectDiagnostics, recordField);
   }
 
   // One force evaluation (pmMethodStep + short-range forces + correctAccelerations).

@@ -217,6 +217,30 @@ def ref_run(cfg: PMConfig, q: P3MConfig | None, pos, vel, mass, sim_length, diag
     return out[:n], out[n:], bool(esc.value)
 
 
+def ref_run_files(cfg: PMConfig, q: P3MConfig | None, pos, vel, mass, sim_length, outdir,
+                  diagnostics=False, record_field=False):
+    """run(StateRecorder(outdir), sim_length, diagnostics, record_field) of the compiled
+    reference, leaving its output files in outdir; returns (escaped, {file name: bytes})."""
+    n = len(mass)
+    st, m = _state(pos, vel), _f32(mass)
+    out = np.zeros((2 * n, 3), np.float32)
+    esc = C.c_int(0)
+    flags = (1 if diagnostics else 0) | (2 if record_field else 0)
+    if q is None:
+        rc = ref().ref_pm_run(C.byref(cfg.c()), n, _ptr(st, C.c_float), _ptr(m, C.c_float),
+                              sim_length, outdir.encode(), _ptr(out, C.c_float), C.byref(esc), flags)
+    else:
+        rc = ref().ref_p3m_run(C.byref(cfg.c()), C.byref(q.c()), n, _ptr(st, C.c_float),
+                               _ptr(m, C.c_float), sim_length, outdir.encode(),
+                               _ptr(out, C.c_float), C.byref(esc), flags)
+    assert rc == 0
+    files = {}
+    for name in sorted(os.listdir(outdir)):
+        with open(os.path.join(outdir, name), "rb") as f:
+            files[name] = f.read()
+    return bool(esc.value), files
+
+
 def ref_chaining_mesh(q: P3MConfig, H, pos_code, y_sorting=1):
     n = len(pos_code)
     pc = _f32(pos_code)

@@ -64,7 +64,8 @@ int ref_pm_accel(const orc_pm_params* p, int n, const float* state, const float*
                  float* acc, float* density, float* potential, float* green);
 int ref_p3m_accel(const orc_pm_params* p, const orc_p3m_params* q, int n, const float* state,
                   const float* masses, float* acc);
-/* run(recorder, sim_length, collect_diagnostics, false) with a StateRecorder writing into
+/* run(recorder, sim_length, flags & 1, flags & 2) (collectDiagnostics, recordField; the last
+ * argument holds the flags) with a StateRecorder writing into
  * outdir (positions.dat, energy.txt, momentum.txt, expected_momentum.txt,
  * angular_momentum.txt). */
 int ref_pm_run(const orc_pm_params* p, int n, const float* state, const float* masses,

@@ -212,7 +212,7 @@ int ref_pm_run(const orc_pm_params* p, int n, const float* state, const float* m
       std::streambuf* old = std::cout.rdbuf();
       std::ostringstream sink;
       std::cout.rdbuf(sink.rdbuf());
-      b.pm->run(rec, sim_length, collect_diagnostics != 0, false);
+      b.pm->run(rec, sim_length, (collect_diagnostics & 1) != 0, (collect_diagnostics & 2) != 0);
       std::cout.rdbuf(old);
     }
     exportRunState(b.pm->getParticles(), p, outdir, n, state_out, escaped);
@@ -236,7 +236,7 @@ int ref_p3m_run(const orc_pm_params* p, const orc_p3m_params* q, int n, const fl
       std::streambuf* old = std::cout.rdbuf();
       std::ostringstream sink;
       std::cout.rdbuf(sink.rdbuf());
-      p3m.run(rec, sim_length, collect_diagnostics != 0, false);
+      p3m.run(rec, sim_length, (collect_diagnostics & 1) != 0, (collect_diagnostics & 2) != 0);
       std::cout.rdbuf(old);
     }
     exportRunState(b.pm->getParticles(), p, outdir, n, state_out, escaped);

@@ -197,6 +197,13 @@ int force(pmgb_pm* h, int kdk, float kick, int drift, int tag, bool timed) {
   return PMGB_OK;
 }
 
+// What a run records right after the drift of the iteration tagged `tag`.
+int after_drift(pmgb_pm* h, int tag) {
+  int rc = diag_after_drift(h, tag);
+  if (rc) return rc;
+  return rec_after_drift(h, tag);
+}
+
 int run_loop(pmgb_pm* h, int sim_length, int* steps_done) {
   PMGB_CUDA_TRY(cudaMemsetAsync(h->flags, 0, sizeof(int), h->st));
   const int big = 0x7FFFFFFF;
@@ -206,12 +213,12 @@ int run_loop(pmgb_pm* h, int sim_length, int* steps_done) {
   // initial force, half kick (setHalfStepVelocities) and the drift of iteration 0
   rc = force(h, 1, 0.5f, 1, 0, false);
   if (rc) return rc;
-  rc = diag_after_drift(h, 0);
+  rc = after_drift(h, 0);
   if (rc) return rc;
   for (int t = 0; t <= sim_length; ++t) {
     rc = force(h, 1, 1.0f, t < sim_length ? 1 : 0, t + 1, false);
     if (rc) return rc;
-    if (t < sim_length && (rc = diag_after_drift(h, t + 1))) return rc;
+    if (t < sim_length && (rc = after_drift(h, t + 1))) return rc;
   }
   int flags[2];
   PMGB_CUDA_TRY(cudaMemcpyAsync(flags, h->flags, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
@@ -414,11 +421,11 @@ int pmgb_pm_advance(pmgb_pm* h, int n_steps, int* steps_done, float* device_ms) 
     if (rc) return rc;
     rc = launch_kick_drift(h->pm[h->cur], h->vi[h->cur], h->acc, h->n, sp, 0.f, 1, h->flags, h->st);
     if (rc) return rc;
-    if ((rc = diag_after_drift(h, 0))) return rc;
+    if ((rc = after_drift(h, 0))) return rc;
     for (int t = 0; t < n_steps; ++t) {
       rc = force(h, 1, 1.0f, t + 1 < n_steps ? 1 : 0, t + 1, false);
       if (rc) return rc;
-      if (t + 1 < n_steps && (rc = diag_after_drift(h, t + 1))) return rc;
+      if (t + 1 < n_steps && (rc = after_drift(h, t + 1))) return rc;
     }
   }
   PMGB_CUDA_TRY(cudaEventRecord(h->ev[5], h->st));
@@ -433,6 +440,28 @@ int pmgb_pm_advance(pmgb_pm* h, int n_steps, int* steps_done, float* device_ms) 
   }
   if (steps_done) *steps_done = n_steps;
   return PMGB_OK;
+}
+
+int pmgb_pm_run_recorded(pmgb_pm* h, pmgb_recorder* rec, int sim_length, int collect_diagnostics,
+                         int record_field, int* steps_done) {
+  if (!h || !rec) return set_error("null handle"), PMGB_EINVAL;
+  if (sim_length < 0) return set_error("negative simLength"), PMGB_EINVAL;
+  if (collect_diagnostics && diag_capacity(h) < sim_length + 1) {
+    int rc = pmgb_pm_set_diagnostics(h, sim_length + 1);
+    if (rc) return rc;
+  }
+  h->rec = rec;
+  h->rec_field = record_field ? 1 : 0;
+  int rc = rec_begin_run(h, h->rec_field);
+  const int rc_run = rc ? rc : run_loop(h, sim_length, steps_done);
+  rc = rc_run == PMGB_OK || rc_run == PMGB_EESCAPED ? rec_end_run(h, collect_diagnostics) : PMGB_OK;
+  h->rec = nullptr;
+  if (rc) return rc;
+  if (rc_run != PMGB_OK && rc_run != PMGB_EESCAPED) return rc_run;
+  rc = pmgb_recorder_flush(rec, nullptr, 0);
+  if (rc) return rc;
+  if (rc_run == PMGB_EESCAPED) set_error("Particle moved outside the computational box.");
+  return rc_run;
 }
 
 int pmgb_pm_run(pmgb_pm* h, int sim_length, int* steps_done) {

@@ -327,6 +327,8 @@ int diag_after_drift(pmgb_pm* h, int tag) {
   return launch_records(h, 1, tag);
 }
 
+int diag_capacity(const pmgb_pm* h) { return h->diag ? h->diag->cap : 0; }
+
 void diag_free(pmgb_pm* h) {
   pmgb_diag* d = h->diag;
   if (!d) return;

@@ -45,6 +45,7 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
 struct pmgb_p3m;
 struct pmgb_closure;
 struct pmgb_diag;
+struct pmgb_recorder;
 
 struct pmgb_pm {
   pmgb_pm_config cfg{};
@@ -76,6 +77,8 @@ struct pmgb_pm {
   float* mass_code = nullptr;  // n floats, code-unit masses in original order
   pmgb_diag* diag = nullptr;   // run diagnostics (diag.cu), null when off
   int equal_mass = 0;          // every particle has the same mass (pair pass folds it)
+  pmgb_recorder* rec = nullptr;  // recorder of the current pmgb_pm_run_recorded, else null
+  int rec_field = 0;
 };
 
 struct pmgb_p3m {
@@ -113,4 +116,10 @@ int diag_run_begin(pmgb_pm* h);
 int diag_before_drift(pmgb_pm* h);
 int diag_after_drift(pmgb_pm* h, int tag);
 void diag_free(pmgb_pm* h);
+int diag_capacity(const pmgb_pm* h);
+
+// StateRecorder output (recorder.cu): frame of the iteration tagged `tag`, run start / end.
+int rec_begin_run(pmgb_pm* h, int record_field);
+int rec_after_drift(pmgb_pm* h, int tag);
+int rec_end_run(pmgb_pm* h, int with_diagnostics);
 }  // namespace pmgb

@@ -132,14 +132,22 @@ class PMMethod:
     def pmMethodStep(self):
         check(lib().pmgb_pm_method_step(self._h))
 
-    def run(self, simLength: int, collectDiagnostics: bool = False):
-        """PMMethod::run without recorder: returns (escaped, steps_done).  collectDiagnostics
-        records the reference's per-iteration diagnostics (read them with ``diagnostics()``);
-        it turns them on with room for this run if they are off or too small."""
+    def run(self, simLength: int, collectDiagnostics: bool = False, stateRecorder=None,
+            recordField: bool = False):
+        """PMMethod::run: returns (escaped, steps_done).  collectDiagnostics records the
+        reference's per-iteration diagnostics (read them with ``diagnostics()``); it turns them
+        on with room for this run if they are off or too small.  With a ``StateRecorder`` the
+        run writes the reference's output files (positions every iteration, the field with
+        recordField, energy / momentum lines with collectDiagnostics) and flushes them."""
         if collectDiagnostics:
             self._ensure_diagnostics(int(simLength) + 1)
         done = C.c_int(0)
-        rc = check(lib().pmgb_pm_run(self._h, int(simLength), C.byref(done)))
+        if stateRecorder is not None:
+            rc = check(lib().pmgb_pm_run_recorded(self._h, stateRecorder._h, int(simLength),
+                                                  int(bool(collectDiagnostics)), int(bool(recordField)),
+                                                  C.byref(done)))
+        else:
+            rc = check(lib().pmgb_pm_run(self._h, int(simLength), C.byref(done)))
         return rc == _lib.PMGB_EESCAPED, done.value
 
     # -- run diagnostics (SimInfo) --
@@ -230,6 +238,49 @@ class PMMethod:
         return dict(zip(["sort", "deposit", "poisson", "interpolation", "pair"], t.tolist()))
 
 
+class StateRecorder:
+    """StateRecorder(particlesCnt, framesCnt, outputDirPath, positionsFile, energyFile,
+    momentumFile, expectedMomentumFile, angularMomentumFile, fieldFile) (reference
+    include/stateRecorder.h:10-21): the reference's output files, written from device frame
+    buffers by a host thread.  An empty file name leaves that output out.  ``withField``
+    reserves device room for recordField frames."""
+
+    def __init__(self, particlesCnt: int, framesCnt: int, outputDirPath,
+                 positionsFile="positions.dat", energyFile="energy.txt",
+                 momentumFile="momentum.txt", expectedMomentumFile="expected_momentum.txt",
+                 angularMomentumFile="angular_momentum.txt", fieldFile="field.dat",
+                 withField: bool = True):
+        names = (C.c_char_p * 6)(*[str(x).encode() for x in (
+            positionsFile, energyFile, momentumFile, expectedMomentumFile, angularMomentumFile,
+            fieldFile)])
+        h = C.c_void_p()
+        check(lib().pmgb_recorder_create(int(particlesCnt), int(framesCnt), str(outputDirPath).encode(),
+                                         names, int(bool(withField)), C.byref(h)))
+        self._h = h
+        self.outputDirPath = str(outputDirPath)
+
+    def flush(self) -> str:
+        buf = C.create_string_buffer(4096)
+        check(lib().pmgb_recorder_flush(self._h, buf, 4096))
+        return buf.value.decode()
+
+    def framesWritten(self) -> int:
+        c = C.c_longlong(0)
+        check(lib().pmgb_recorder_frames_written(self._h, C.byref(c)))
+        return int(c.value)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            check(lib().pmgb_recorder_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def fp32_peak_tflops() -> float:
     """Measured FP32 FMA throughput of the current GPU (TFLOP/s)."""
     t = C.c_float(0)
@@ -276,9 +327,12 @@ class P3MMethod:
         """pmMethodStep + calculateShortRangeForces + correctAccelerations."""
         check(lib().pmgb_p3m_force(self._h))
 
-    def run(self, simLength: int, collectDiagnostics: bool = False):
-        """P3MMethod::run without recorder: returns (escaped, steps_done); diagnostics as
-        PMMethod.run (read them with ``pm.diagnostics()``)."""
+    def run(self, simLength: int, collectDiagnostics: bool = False, stateRecorder=None,
+            recordField: bool = False):
+        """P3MMethod::run: returns (escaped, steps_done); diagnostics and recorder as
+        PMMethod.run (read the diagnostics with ``pm.diagnostics()``)."""
+        if stateRecorder is not None:
+            return self.pm.run(simLength, collectDiagnostics, stateRecorder, recordField)
         if collectDiagnostics:
             self.pm._ensure_diagnostics(int(simLength) + 1)
         done = C.c_int(0)

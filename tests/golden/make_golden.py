@@ -1,8 +1,8 @@
 """Generates tests/golden/*.npz from the reference's own CPU code (oracle/_ref/libpsref.so,
 compiled from the reference sources by oracle/Makefile).
 
-Run where the reference sources exist:  python tests/golden/make_golden.py [diagnostics]
-(with "diagnostics", only diagnostics.npz is rewritten).
+Run where the reference sources exist:  python tests/golden/make_golden.py [diagnostics|recorder]
+(with an argument, only diagnostics.npz or recorder.npz is rewritten).
 Every case is a small seeded input; each fixture stores the inputs, the settings and the
 reference's outputs (float32), so tests on a machine without the reference still compare
 against the reference itself.
@@ -88,6 +88,35 @@ def diagnostics_fixture():
                            sim_length=np.int32(6), **_cfg_arrays(cfg))
     np.savez_compressed(os.path.join(HERE, "diagnostics.npz"),
                         **{f"{c}/{k}": a for c, dd in cases.items() for k, a in dd.items()})
+
+
+def recorder_fixture():
+    """The reference's StateRecorder files (raw bytes) of PM runs with collectDiagnostics and
+    recordField: one with an external field, one stopped by an escaped particle."""
+    import tempfile
+    H = 30.0 / 16
+    p, v, m = inputs(70, 800, 8.0, 22.0)
+    out = {}
+    cases = []
+    cfg = O.PMConfig(grid=(32, 32, 32), box=(30.0, 30.0, 30.0), H=H, DT=0.1, G=1.0,
+                     interpolation=2, finite_diff=1, greens=0, diameter=0.0,
+                     ext=(15.0, 15.0, 15.0, 3.0, 0.5, 1.0))
+    cases.append(("ext", cfg, p, v, 5))
+    pe, ve = p.copy(), v.copy()
+    pe[:10, 0] = 29.6
+    ve[:10, 0] = 0.05 * 30
+    cfg2 = O.PMConfig(grid=(32, 32, 32), box=(30.0, 30.0, 30.0), H=H, DT=0.1, G=1.0,
+                      interpolation=1, finite_diff=0, greens=0, diameter=0.0)
+    cases.append(("escape", cfg2, pe, ve, 6))
+    for name, c, pp, vv, steps in cases:
+        with tempfile.TemporaryDirectory() as d:
+            esc, files = O.ref_run_files(c, None, pp, vv, m, steps, d, diagnostics=True,
+                                         record_field=True)
+        out[name] = dict(pos=pp, vel=vv, mass=m, escaped=np.int32(esc), sim_length=np.int32(steps),
+                         **_cfg_arrays(c),
+                         **{f"file:{k}": np.frombuffer(b, np.uint8) for k, b in files.items()})
+    np.savez_compressed(os.path.join(HERE, "recorder.npz"),
+                        **{f"{c}/{k}": a for c, dd in out.items() for k, a in dd.items()})
 
 
 def main():
@@ -199,6 +228,9 @@ def _p3m_arrays(q):
 if __name__ == "__main__":
     if sys.argv[1:] == ["diagnostics"]:
         diagnostics_fixture()
+    elif sys.argv[1:] == ["recorder"]:
+        recorder_fixture()
     else:
         main()
         diagnostics_fixture()
+        recorder_fixture()
