@@ -187,6 +187,22 @@ int pmgb_pm_set_diagnostics(pmgb_pm* pm, int capacity);
  * (records beyond the capacity are dropped).  *count = 0 when diagnostics are off. */
 int pmgb_pm_get_diagnostics(pmgb_pm* pm, double* records, int max_records, int* count);
 
+/* ---------------------------------------------------------------- samplers ----------- */
+
+/* PlummerSampler(seed).sample(center, a, rMax, M, G, n) (source/plummerSampler.cpp:11-83; the
+ * argument order of its definition, which the reference's callers use) and
+ * DiskSamplerLinear(seed).sample(center, rb, mb, rd, md, thickness, G, n, r0)
+ * (source/diskSamplerLinear.cpp:10-74), on the device, one thread per particle, drawing the
+ * reference's own random stream (std::default_random_engine(seed), i.e. minstd_rand0, through
+ * uniform_real_distribution<float>).  offset = numbers already drawn from that engine (6 per
+ * Plummer particle, 3 per disk particle of earlier sample() calls on the same sampler).
+ * state = 6n floats (host): n positions then n velocities. */
+int pmgb_sample_plummer(unsigned int seed, unsigned long long offset, const float* center, float a,
+                        float r_max, float M, float G, int n, float* state);
+int pmgb_sample_disk_linear(unsigned int seed, unsigned long long offset, const float* center,
+                            float rb, float mb, float rd, float md, float thickness, float G, int n,
+                            float r0, float* state);
+
 /* ---------------------------------------------------------------- StateRecorder ------ */
 
 /* StateRecorder(particlesCnt, framesCnt, outputDirPath, positionsFile, energyFile,

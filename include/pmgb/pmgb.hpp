@@ -5,9 +5,10 @@
 // member functions (include/pmMethod.h:12-46, include_gpu/PMMethodGPU.h:12-55,
 // include/p3mMethod.h:11-31), same enums (include/pmConfig.h:3-5, include/greensFunctions.h:7),
 // and the same error behaviour (std::invalid_argument for bad enums / arguments, a printed
-// message and an early return when a particle leaves the box).  Two differences a device path
-// needs: the external field is described by `ExternalField` (sphRadDecrField parameters, or
-// none) instead of a host std::function, and run() takes no StateRecorder.
+// message and an early return when a particle leaves the box), plus the reference's
+// StateRecorder, PlummerSampler and DiskSamplerLinear.  One difference a device path needs: the
+// external field is described by `ExternalField` (sphRadDecrField parameters, or none) instead
+// of a host std::function.
 #pragma once
 
 #include <cstdio>
@@ -24,6 +25,7 @@ namespace pmgb {
 struct Vec3 {
   float x{}, y{}, z{};
 };
+static_assert(sizeof(Vec3) == 3 * sizeof(float), "Vec3 is three packed floats");
 
 enum class InterpolationScheme { NGP = PMGB_NGP, CIC = PMGB_CIC, TSC = PMGB_TSC };
 enum class FiniteDiffScheme { TWO_POINT = PMGB_TWO_POINT, FOUR_POINT = PMGB_FOUR_POINT };
@@ -35,8 +37,6 @@ enum class GreensFunction {
 };
 enum class CloudShape { S1 = PMGB_S1, S2 = PMGB_S2 };
 
-// The reference's Particle (include/particle.h:5-15) without the per-neighbour P3M slots,
-// which the device path does not need.
 // One record of the run diagnostics (PMGB_DIAG_* layout of pmgb.h): what SimInfo computes
 // (reference source/simInfo.cpp:50-127) after each drift of a run with collectDiagnostics.
 struct DiagnosticsRecord {
@@ -48,6 +48,46 @@ struct DiagnosticsRecord {
   double externalPotentialEnergy;
 };
 static_assert(sizeof(DiagnosticsRecord) == PMGB_DIAG_WIDTH * sizeof(double), "record layout");
+
+// PlummerSampler / DiskSamplerLinear with the reference's interface (include/plummerSampler.h,
+// include/diskSamplerLinear.h): the state of n particles (n positions then n velocities),
+// sampled on the device from the reference's own random stream; successive sample() calls
+// continue the stream like the reference's engine.
+class PlummerSampler {
+ public:
+  explicit PlummerSampler(unsigned int seed = 0) : seed(seed) {}
+  std::vector<Vec3> sample(Vec3 center, float a, float rMax, float M, float G, int n) {
+    std::vector<Vec3> state(2 * size_t(n));
+    const float c[3] = {center.x, center.y, center.z};
+    int rc = pmgb_sample_plummer(seed, draws, c, a, rMax, M, G, n, reinterpret_cast<float*>(state.data()));
+    if (rc != PMGB_OK) throw std::invalid_argument(pmgb_last_error());
+    draws += 6ull * (unsigned long long)n;
+    return state;
+  }
+
+ private:
+  unsigned int seed;
+  unsigned long long draws = 0;
+};
+
+class DiskSamplerLinear {
+ public:
+  explicit DiskSamplerLinear(unsigned int seed = 0) : seed(seed) {}
+  std::vector<Vec3> sample(Vec3 center, float rb, float mb, float rd, float md, float thickness,
+                           float G, int n, float r0 = 0.0f) {
+    std::vector<Vec3> state(2 * size_t(n));
+    const float c[3] = {center.x, center.y, center.z};
+    int rc = pmgb_sample_disk_linear(seed, draws, c, rb, mb, rd, md, thickness, G, n, r0,
+                                     reinterpret_cast<float*>(state.data()));
+    if (rc != PMGB_OK) throw std::invalid_argument(pmgb_last_error());
+    draws += 3ull * (unsigned long long)n;
+    return state;
+  }
+
+ private:
+  unsigned int seed;
+  unsigned long long draws = 0;
+};
 
 // StateRecorder with the reference's constructor (include/stateRecorder.h:10-21); the files
 // and their formats are the reference's.  maxRecords (the reference's write-batch size) has no
@@ -80,6 +120,8 @@ class StateRecorder {
   pmgb_recorder* h = nullptr;
 };
 
+// The reference's Particle (include/particle.h:5-15) without the per-neighbour P3M slots,
+// which the device path does not need.
 struct Particle {
   Vec3 position, velocity, acceleration;
   float mass{};

@@ -386,3 +386,36 @@ def port_time_steps(cfg: PMConfig, q: P3MConfig | None, pos, vel, mass, steps, n
                                 pair_stride, _ptr(out, C.c_double))
     assert rc == 0
     return dict(est=out[0], pm=out[1], cells=out[2], pair_sampled=out[3])
+
+
+# ----------------------------------------------------------------- samplers ---
+def ref_sample_plummer(seed, center, a, r_max, M, G, n):
+    out = np.zeros((2 * n, 3), np.float32)
+    c = _f32(center)
+    ref().ref_sample_plummer(C.c_uint(seed), _ptr(c, C.c_float), C.c_float(a), C.c_float(r_max),
+                             C.c_float(M), C.c_float(G), n, _ptr(out, C.c_float))
+    return out
+
+
+def ref_sample_disk_linear(seed, center, rb, mb, rd, md, thickness, G, n, r0=0.0):
+    out = np.zeros((2 * n, 3), np.float32)
+    c = _f32(center)
+    ref().ref_sample_disk_linear(C.c_uint(seed), _ptr(c, C.c_float), C.c_float(rb), C.c_float(mb),
+                                 C.c_float(rd), C.c_float(md), C.c_float(thickness), C.c_float(G), n,
+                                 C.c_float(r0), _ptr(out, C.c_float))
+    return out
+
+
+def minstd_uniforms(seed, count, offset=0):
+    """The float uniforms std::uniform_real_distribution<float>(0, 1) draws from
+    std::default_random_engine(seed) in libstdc++ (minstd_rand0; generate_canonical<float, 24>
+    takes one engine value per number): u = float(x - 1) / float(2^31 - 2), below 1."""
+    m, a = 2147483647, 16807
+    x = seed % m or 1
+    x = x * pow(a, offset, m) % m
+    out = np.empty(count, np.float32)
+    for k in range(count):
+        x = x * a % m
+        u = np.float32(np.float32(x - 1) / np.float32(2147483646.0))
+        out[k] = u if u < 1 else np.nextafter(np.float32(1), np.float32(0))
+    return out

@@ -81,6 +81,12 @@ int ref_chaining_mesh(const orc_p3m_params* q, float H, int n, const float* pos_
 int ref_pp_accel(int n, const float* pos, const float* masses, float G, float eps, float* acc);
 /* P3MMethod's FTable and deltaSquared (source/p3mMethod.cpp:42-47, 275-294). */
 int ref_sr_table(const orc_p3m_params* q, float H, float* table /*500*/, float* delta_sq);
+/* PlummerSampler(seed).sample(center, a, rMax, M, G, n) and DiskSamplerLinear(seed).sample(
+ * center, rb, mb, rd, md, thickness, G, n, r0): 2n xyz triplets, positions then velocities. */
+int ref_sample_plummer(unsigned int seed, const float* center, float a, float r_max, float M,
+                       float G, int n, float* state_out);
+int ref_sample_disk_linear(unsigned int seed, const float* center, float rb, float mb, float rd,
+                           float md, float thickness, float G, int n, float r0, float* state_out);
 
 /* ---- port (oracle/port.cpp); prec = 0 float, 1 double ---- */
 int port_pm_accel(int prec, const orc_pm_params* p, int n, const float* state,

@@ -316,3 +316,42 @@ int ref_sr_table(const orc_p3m_params* q, float H, float* table, float* delta_sq
 }
 
 }  // extern "C"
+
+/* ---- samplers: PlummerSampler(seed).sample(center, a, rMax, M, G, n) (the parameter order of
+ * its definition, source/plummerSampler.cpp:11-16) and DiskSamplerLinear(seed).sample(...)
+ * (source/diskSamplerLinear.cpp:10-33); state_out = 2n xyz triplets (positions, velocities). */
+#include "diskSamplerLinear.h"
+#include "plummerSampler.h"
+
+extern "C" int ref_sample_plummer(unsigned int seed, const float* c, float a, float r_max, float M,
+                                  float G, int n, float* state_out) {
+  PlummerSampler s(seed);
+  Vec3 center;
+  center.x = c[0];
+  center.y = c[1];
+  center.z = c[2];
+  auto st = s.sample(center, a, r_max, M, G, n);
+  for (int i = 0; i < 2 * n; ++i) {
+    state_out[3 * i] = st[i].x;
+    state_out[3 * i + 1] = st[i].y;
+    state_out[3 * i + 2] = st[i].z;
+  }
+  return 0;
+}
+
+extern "C" int ref_sample_disk_linear(unsigned int seed, const float* c, float rb, float mb, float rd,
+                                      float md, float thickness, float G, int n, float r0,
+                                      float* state_out) {
+  DiskSamplerLinear s(seed);
+  Vec3 center;
+  center.x = c[0];
+  center.y = c[1];
+  center.z = c[2];
+  auto st = s.sample(center, rb, mb, rd, md, thickness, G, n, r0);
+  for (int i = 0; i < 2 * n; ++i) {
+    state_out[3 * i] = st[i].x;
+    state_out[3 * i + 1] = st[i].y;
+    state_out[3 * i + 2] = st[i].z;
+  }
+  return 0;
+}

@@ -1,6 +1,8 @@
 """GB300-native PM / P3M force-and-step path (CUDA sm_103a behind the C ABI of include/pmgb.h)."""
-from .methods import (CloudShape, FiniteDiffScheme, GreensFunction, InterpolationScheme,
-                      LearnedClosure, P3MMethod, PMMethod, SphRadDecrField, StateRecorder)
+from .methods import (CloudShape, DiskSamplerLinear, FiniteDiffScheme, GreensFunction,
+                      InterpolationScheme, LearnedClosure, P3MMethod, PlummerSampler, PMMethod,
+                      SphRadDecrField, StateRecorder)
 
-__all__ = ["PMMethod", "P3MMethod", "LearnedClosure", "StateRecorder", "InterpolationScheme",
-           "FiniteDiffScheme", "GreensFunction", "CloudShape", "SphRadDecrField"]
+__all__ = ["PMMethod", "P3MMethod", "LearnedClosure", "StateRecorder", "PlummerSampler",
+           "DiskSamplerLinear", "InterpolationScheme", "FiniteDiffScheme", "GreensFunction",
+           "CloudShape", "SphRadDecrField"]

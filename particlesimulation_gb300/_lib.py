@@ -21,7 +21,8 @@ EXPORTS = [
     "pmgb_pm_get_density", "pmgb_pm_get_potential", "pmgb_pm_get_greens_function",
     "pmgb_pm_stage_times", "pmgb_pm_size", "pmgb_pm_set_diagnostics", "pmgb_pm_get_diagnostics",
     "pmgb_recorder_create", "pmgb_recorder_destroy", "pmgb_recorder_flush",
-    "pmgb_recorder_frames_written", "pmgb_pm_run_recorded",
+    "pmgb_recorder_frames_written", "pmgb_pm_run_recorded", "pmgb_sample_plummer",
+    "pmgb_sample_disk_linear",
     "pmgb_p3m_create", "pmgb_p3m_destroy",
     "pmgb_p3m_force", "pmgb_p3m_run", "pmgb_p3m_get_cell_lists", "pmgb_p3m_get_sr_table",
     "pmgb_p3m_pair_count", "pmgb_fp32_peak_probe", "pmgb_kernel_launches",
@@ -95,6 +96,10 @@ def lib() -> C.CDLL:
         L.pmgb_recorder_flush.argtypes = [vp, C.c_char_p, C.c_int]
         L.pmgb_recorder_frames_written.argtypes = [vp, C.POINTER(C.c_longlong)]
         L.pmgb_pm_run_recorded.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, ip]
+        L.pmgb_sample_plummer.argtypes = [C.c_uint, C.c_ulonglong, fp, C.c_float, C.c_float, C.c_float,
+                                          C.c_float, C.c_int, fp]
+        L.pmgb_sample_disk_linear.argtypes = [C.c_uint, C.c_ulonglong, fp, C.c_float, C.c_float, C.c_float,
+                                              C.c_float, C.c_float, C.c_float, C.c_int, C.c_float, fp]
         L.pmgb_p3m_create.argtypes = [vp, C.POINTER(P3MConfigC), C.POINTER(vp)]
         L.pmgb_p3m_destroy.argtypes = [vp]
         L.pmgb_p3m_force.argtypes = [vp]

@@ -238,6 +238,42 @@ class PMMethod:
         return dict(zip(["sort", "deposit", "poisson", "interpolation", "pair"], t.tolist()))
 
 
+class PlummerSampler:
+    """PlummerSampler(seed) (reference include/plummerSampler.h): ``sample(center, a, rMax, M,
+    G, n)`` returns the (2n, 3) state (positions, velocities), drawn on the GPU from the
+    reference's own random stream; successive calls continue the stream as the reference's
+    engine does."""
+
+    def __init__(self, seed: int = 0):
+        self.seed = int(seed)
+        self.draws = 0
+
+    def sample(self, center, a, rMax, M, G, n: int):
+        out = np.zeros((2 * int(n), 3), np.float32)
+        c = _f32(center).reshape(3)
+        check(lib().pmgb_sample_plummer(C.c_uint(self.seed), C.c_ulonglong(self.draws), _fp(c), a, rMax,
+                                        M, G, int(n), _fp(out)))
+        self.draws += 6 * int(n)
+        return out
+
+
+class DiskSamplerLinear:
+    """DiskSamplerLinear(seed) (reference include/diskSamplerLinear.h): ``sample(center, rb, mb,
+    rd, md, thickness, G, n, r0=0)`` as PlummerSampler.sample."""
+
+    def __init__(self, seed: int = 0):
+        self.seed = int(seed)
+        self.draws = 0
+
+    def sample(self, center, rb, mb, rd, md, thickness, G, n: int, r0: float = 0.0):
+        out = np.zeros((2 * int(n), 3), np.float32)
+        c = _f32(center).reshape(3)
+        check(lib().pmgb_sample_disk_linear(C.c_uint(self.seed), C.c_ulonglong(self.draws), _fp(c), rb, mb,
+                                            rd, md, thickness, G, int(n), r0, _fp(out)))
+        self.draws += 3 * int(n)
+        return out
+
+
 class StateRecorder:
     """StateRecorder(particlesCnt, framesCnt, outputDirPath, positionsFile, energyFile,
     momentumFile, expectedMomentumFile, angularMomentumFile, fieldFile) (reference

@@ -1,8 +1,9 @@
 """Generates tests/golden/*.npz from the reference's own CPU code (oracle/_ref/libpsref.so,
 compiled from the reference sources by oracle/Makefile).
 
-Run where the reference sources exist:  python tests/golden/make_golden.py [diagnostics|recorder]
-(with an argument, only diagnostics.npz or recorder.npz is rewritten).
+Run where the reference sources exist:
+    python tests/golden/make_golden.py [diagnostics|recorder|samplers]
+(with an argument, only that fixture is rewritten).
 Every case is a small seeded input; each fixture stores the inputs, the settings and the
 reference's outputs (float32), so tests on a machine without the reference still compare
 against the reference itself.
@@ -119,6 +120,21 @@ def recorder_fixture():
                         **{f"{c}/{k}": a for c, dd in out.items() for k, a in dd.items()})
 
 
+def samplers_fixture():
+    """PlummerSampler(42) and DiskSamplerLinear(42) samples of the reference with the parameters
+    of its plummerPM / galaxy demos (source/demos.cpp:361-372, 1369-1384); the disk also with
+    an inner radius r0 (the galaxy-collision demo) and with 2n particles in one call (its second
+    half is what a second sample() call of the same sampler returns)."""
+    n = 5000
+    out = {
+        "plummer": O.ref_sample_plummer(42, (30, 30, 30), 2.0, 15.0, 1.0, 4.5e-3, n),
+        "disk": O.ref_sample_disk_linear(42, (30, 30, 15), 3.0, 60.0, 15.0, 15.0, 0.3, 4.5e-3, n),
+        "disk_r0": O.ref_sample_disk_linear(7, (30, 30, 15), 3.0, 60.0, 15.0, 15.0, 0.3, 4.5e-3, n, 3.0),
+        "disk_2n": O.ref_sample_disk_linear(42, (30, 30, 15), 3.0, 60.0, 15.0, 15.0, 0.3, 4.5e-3, 2 * n),
+    }
+    np.savez_compressed(os.path.join(HERE, "samplers.npz"), **out)
+
+
 def main():
     assert O.build_ref(), "reference sources not found"
     os.makedirs(HERE, exist_ok=True)
@@ -230,7 +246,10 @@ if __name__ == "__main__":
         diagnostics_fixture()
     elif sys.argv[1:] == ["recorder"]:
         recorder_fixture()
+    elif sys.argv[1:] == ["samplers"]:
+        samplers_fixture()
     else:
         main()
         diagnostics_fixture()
         recorder_fixture()
+        samplers_fixture()
