@@ -52,6 +52,8 @@ def parse():
                     help="skip the plain-P3M vs learned-closure comparison")
     ap.add_argument("--no-ensemble", action="store_true",
                     help="skip the 64-system ensemble measurement")
+    ap.add_argument("--no-reference-scenarios", action="store_true",
+                    help="skip the reference's own timing scenarios (run by the scenario CLI)")
     ap.add_argument("--no-pm-hbm", action="store_true",
                     help="skip the HBM-roofline measurement of the PM path on the 256^3 workload")
     ap.add_argument("--closure-epochs", type=int, default=10)
@@ -321,6 +323,9 @@ def run_ours(args):
     pm_hbm = None
     if not args.no_pm_hbm and args.workload == "disk_p3m":
         pm_hbm = pm_hbm_bench(args, rank, world)
+    scenarios = None
+    if rank == 0 and world == 1 and not args.no_reference_scenarios and args.workload == "disk_p3m":
+        scenarios = reference_scenarios()
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -329,7 +334,8 @@ def run_ours(args):
                 "config": {**config_of(w), "l2": "256 MB L2 flush before every timed step"},
                 "e2e": e2e, "roofline": roofline, "roofline_pm": roofline_pm,
                 "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
-                "closure": closure, "ensemble": ensemble, "pm_hbm": pm_hbm, "impl": "ours"}
+                "closure": closure, "ensemble": ensemble, "pm_hbm": pm_hbm,
+                "reference_scenarios": scenarios, "impl": "ours"}
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -495,6 +501,48 @@ def pm_hbm_bench(args, rank=0, world=1):
                                          "bytes_per_step": byts, "peak_source": src},
             "stage_ms": {k: round(v, 4) for k, v in stage.items() if k not in ("pair",)},
             "l2": "working set larger than L2"}
+
+
+# The reference's own published timings of its timing scenarios (whole run of
+# galaxySimulationPMTiming / galaxySimulationP3MTiming, source/demos.cpp:779-836, 953-1016:
+# disk + bulge, 128x128x64, TSC, 101 resp. 26 iterations with diagnostics and StateRecorder
+# output), seconds per N, from its timing/pm_time_cpu.txt, timing/pm_time_gpu.txt and
+# timing/p3m_time.txt (hardware not stated there).
+REF_TIMING = {
+    "galaxy-sim-pm-timing": {
+        "reference_gpu_s": [0.931208, 1.03497, 1.15184, 1.32805, 1.44811, 1.48474, 1.60336, 1.75799, 1.82338],
+        "reference_cpu_s": [5.54486, 5.76422, 5.96315, 6.15246, 6.3574, 6.58436, 6.89709, 7.05142, 7.10521],
+    },
+    "galaxy-sim-p3m-timing": {
+        "reference_cpu_s": [10.8499, 12.9906, 17.6909, 20.7594, 26.9943, 34.7315, 40.1174, 48.9757, 60.7412],
+    },
+}
+
+
+def reference_scenarios():
+    """The reference's timing scenarios run by the scenario command line on this GPU (same
+    samplers, seeds, settings, diagnostics and output files), wall-clock seconds of each run as
+    the reference measures them, next to its published seconds."""
+    from particlesimulation_gb300 import build as B
+    exe = B.build_demos()
+    out = {}
+    for opt, ref in REF_TIMING.items():
+        with tempfile.TemporaryDirectory() as d:
+            r = subprocess.run([exe, opt, d], capture_output=True, text=True, timeout=900)
+        if r.returncode != 0:
+            out[opt] = {"error": r.stderr.strip()[-300:]}
+            continue
+        rows = [line.split() for line in r.stdout.splitlines() if len(line.split()) == 2
+                and line.split()[0].isdigit()]
+        ns = [int(a) for a, _ in rows]
+        secs = [float(b) for _, b in rows]
+        entry = {"n": ns, "seconds": secs, **ref,
+                 "escaped": "outside the computational box" in r.stdout}
+        for k, v in ref.items():
+            if len(v) == len(secs):
+                entry["speedup_vs_" + k[:-2]] = [round(a / b, 1) for a, b in zip(v, secs)]
+        out[opt] = entry
+    return out
 
 
 def run_reference(args):

@@ -75,5 +75,27 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB
 
 
+DEMOS_SRC = os.path.join(PKG, "demos", "pmgb_demos.cpp")
+DEMOS_BIN = os.path.join(PKG, "pmgb_demos")
+
+
+def build_demos(force: bool = False) -> str:
+    """The scenario command line (demos/pmgb_demos.cpp, the reference's demos on the facade),
+    linked against libpmgb.so with an rpath to this directory."""
+    lib = build()
+    deps = [DEMOS_SRC, lib, os.path.join(ROOT, "include", "pmgb", "pmgb.hpp")]
+    if not force and os.path.exists(DEMOS_BIN) and all(
+            os.path.getmtime(d) <= os.path.getmtime(DEMOS_BIN) for d in deps):
+        return DEMOS_BIN
+    cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+           DEMOS_SRC, "-o", DEMOS_BIN + ".tmp", f"-L{PKG}", "-lpmgb", f"-Wl,-rpath,{PKG}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"demos build failed:\n{r.stderr}")
+    os.replace(DEMOS_BIN + ".tmp", DEMOS_BIN)
+    return DEMOS_BIN
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose=True))
+    print(build_demos())

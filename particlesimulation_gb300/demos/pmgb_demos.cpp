@@ -1,0 +1,188 @@
+// pmgb_demos.cpp - the reference's PM / P3M simulation scenarios (source/demos.cpp, selected by
+// the command line of source/main.cpp:23-62) on the GB300 path, written against the drop-in
+// facade (include/pmgb/pmgb.hpp) exactly as the reference's demos are written against its
+// classes: same samplers and seeds, same settings, same StateRecorder output files.
+//
+//   pmgb_demos <option> [output dir]
+//
+// Options: galaxy-sim-pm, galaxy-sim-p3m, galaxy-collision-sim-pm, galaxy-collision-sim-p3m,
+// cluster-sim-pm, cluster-sim-p3m, galaxy-sim-pm-timing, galaxy-sim-p3m-timing.
+// Differences from the reference's scenarios, all deliberate: the external field is passed as a
+// description (the GPU path has no host callbacks); galaxy-sim-p3m uses the reference's CPU
+// settings (S1-optimal influence function, a = 3H), which its CUDA build replaced by the
+// discrete Laplacian; cluster-sim-p3m runs P3M (the reference builds the P3MMethod and then
+// runs the plain PM method).
+#include <chrono>
+#include <cstdio>
+#include <functional>
+#include <iostream>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "pmgb/pmgb.hpp"
+
+using namespace pmgb;
+
+namespace {
+
+Vec3 v3(float x, float y, float z) { return Vec3{x, y, z}; }
+
+// galaxy-sim-pm (galaxySimulationPM, source/demos.cpp:729-777): linear disk + external bulge
+void galaxySimulationPM(const std::string& out, int n = 50000, int simLength = 200, bool timing = false) {
+  const Vec3 center = v3(30, 30, 15);
+  const float rb = 3.0f, mb = 60.0f, rd = 15.0f, md = 15.0f, thickness = 0.3f, G = 4.5e-3f;
+  DiskSamplerLinear diskSampler(42);
+  std::vector<Vec3> state = diskSampler.sample(center, rb, mb, rd, md, thickness, G, n);
+  std::vector<float> masses(n, md / n);
+  const auto gridPoints = std::make_tuple(128, 128, 64);
+  const auto box = std::make_tuple(60.0f, 60.0f, 30.0f);
+  const float H = std::get<0>(box) / (std::get<0>(gridPoints) / 2), DT = 1;
+  PMMethodGPU pm(state, masses, box, ExternalField::sphRadDecr(center, rb, mb, G), H, DT, G,
+                 InterpolationScheme::TSC, FiniteDiffScheme::TWO_POINT,
+                 GreensFunction::DISCRETE_LAPLACIAN, 0, gridPoints);
+  StateRecorder stateRecorder(n, simLength + 1, out);
+  const auto t0 = std::chrono::high_resolution_clock::now();
+  pm.run(stateRecorder, simLength, true /*diagnostics*/);
+  const std::chrono::duration<double> dt = std::chrono::high_resolution_clock::now() - t0;
+  if (timing) std::cout << n << ' ' << dt.count() << std::endl;
+}
+
+// galaxy-sim-p3m (galaxySimulationP3M, source/demos.cpp:897-951)
+void galaxySimulationP3M(const std::string& out, int n = 50000, int simLength = 200, bool timing = false) {
+  const Vec3 center = v3(30, 30, 15);
+  const float rb = 3.0f, mb = 60.0f, rd = 15.0f, md = 15.0f, thickness = 0.3f, G = 4.5e-3f;
+  DiskSamplerLinear diskSampler(42);
+  std::vector<Vec3> state = diskSampler.sample(center, rb, mb, rd, md, thickness, G, n);
+  std::vector<float> masses(n, md / n);
+  const auto gridPoints = std::make_tuple(128, 128, 64);
+  const auto box = std::make_tuple(60.0f, 60.0f, 30.0f);
+  const float H = std::get<0>(box) / (std::get<0>(gridPoints) / 2), DT = 1;
+  const float a = 3 * H;
+  PMMethodGPU pm(state, masses, box, ExternalField::sphRadDecr(center, rb, mb, G), H, DT, G,
+                 InterpolationScheme::TSC, FiniteDiffScheme::TWO_POINT, GreensFunction::S1_OPTIMAL, a,
+                 gridPoints);
+  const float re = 0.7f * a, softeningLength = 1.5f;
+  P3MMethod p3m(pm, box, re, a, H, softeningLength, CloudShape::S1);
+  StateRecorder stateRecorder(n, simLength + 1, out);
+  const auto t0 = std::chrono::high_resolution_clock::now();
+  p3m.run(stateRecorder, simLength, true /*diagnostics*/);
+  const std::chrono::duration<double> dt = std::chrono::high_resolution_clock::now() - t0;
+  if (timing) std::cout << n << ' ' << dt.count() << std::endl;
+}
+
+// Two disks, the second scaled down by 1.5, each with a central point mass
+// (galaxyCollisionPM / galaxyCollisionP3M, source/demos.cpp:838-895, 1018-1080).
+void collisionState(std::vector<Vec3>& state, std::vector<float>& masses, int n) {
+  const Vec3 c1 = v3(40, 30, 15), c2 = v3(80, 30, 15);
+  const float rb = 3.0f, mb = 60.0f, rd = 15.0f, md = 15.0f, thickness = 0.3f, G = 4.5e-3f;
+  DiskSamplerLinear diskSampler(42);
+  std::vector<Vec3> s1 = diskSampler.sample(c1, rb, mb, rd, md, thickness, G, n, rb);
+  std::vector<float> m1(n, md / n);
+  s1[0] = c1;
+  s1[n] = v3(0, 0, 0);
+  m1[0] = 60.0f;
+  std::vector<Vec3> s2 = diskSampler.sample(c2, rb / 1.5f, mb / 1.5f, rd / 1.5f, md / 1.5f, thickness,
+                                            G, n, rb / 1.5f);
+  std::vector<float> m2(n, md / n);
+  s2[0] = c2;
+  s2[n] = v3(0, 0, 0);
+  m2[0] = 60.0f / 1.5f;
+  state.assign(4 * size_t(n), Vec3{});
+  masses.assign(2 * size_t(n), 0.f);
+  for (int i = 0; i < n; ++i) {
+    state[i] = s1[i];
+    state[i + 2 * n] = s1[i + n];
+    masses[i] = m1[i];
+    state[i + n] = s2[i];
+    state[i + 3 * n] = s2[i + n];
+    masses[i + n] = m2[i];
+  }
+}
+
+void galaxyCollision(const std::string& out, bool p3mRun) {
+  const int n = 30000, simLength = 400;
+  const float G = 4.5e-3f;
+  std::vector<Vec3> state;
+  std::vector<float> masses;
+  collisionState(state, masses, n);
+  const auto gridPoints = std::make_tuple(128, 128, 64);
+  const auto box = std::make_tuple(120.0f, 120.0f, 60.0f);
+  const float H = std::get<0>(box) / (std::get<0>(gridPoints) / 2), DT = 1;
+  const float a = 3 * H;
+  PMMethodGPU pm(state, masses, box, ExternalField::none(), H, DT, G, InterpolationScheme::TSC,
+                 FiniteDiffScheme::TWO_POINT,
+                 p3mRun ? GreensFunction::S1_OPTIMAL : GreensFunction::DISCRETE_LAPLACIAN,
+                 p3mRun ? a : 0.0f, gridPoints);
+  StateRecorder stateRecorder(2 * n, simLength + 1, out);
+  if (p3mRun) {
+    P3MMethod p3m(pm, box, 0.7f * a, a, H, 1.5f, CloudShape::S1);
+    p3m.run(stateRecorder, simLength, true /*diagnostics*/);
+  } else {
+    pm.run(stateRecorder, simLength, true /*diagnostics*/);
+  }
+}
+
+// cluster-sim-pm / cluster-sim-p3m (plummerPM / plummerP3M, source/demos.cpp:1369-1452)
+void plummer(const std::string& out, bool p3mRun) {
+  const Vec3 center = v3(30, 30, 30);
+  const float a = 2, rMax = 15, M = 1.0f, G = 4.5e-3f;
+  const int n = 10000, simLength = 200;
+  PlummerSampler sampler(42);
+  std::vector<Vec3> state = sampler.sample(center, a, rMax, M, G, n);
+  std::vector<float> masses(n, M / n);
+  const auto gridPoints = std::make_tuple(128, 128, 128);
+  const auto box = std::make_tuple(60.0f, 60.0f, 60.0f);
+  const float H = std::get<0>(box) / (std::get<0>(gridPoints) / 2), DT = 1;
+  const float particleDiam = 3 * H;
+  PMMethodGPU pm(state, masses, box, ExternalField::none(), H, DT, G, InterpolationScheme::TSC,
+                 FiniteDiffScheme::TWO_POINT,
+                 p3mRun ? GreensFunction::S1_OPTIMAL : GreensFunction::DISCRETE_LAPLACIAN,
+                 p3mRun ? particleDiam : 0.0f, gridPoints);
+  StateRecorder stateRecorder(n, simLength + 1, out);
+  if (p3mRun) {
+    P3MMethod p3m(pm, box, 0.7f * a, particleDiam, H, 0.5f, CloudShape::S1);
+    p3m.run(stateRecorder, simLength, true /*diagnostics*/);
+  } else {
+    pm.run(stateRecorder, simLength, true /*diagnostics*/);
+  }
+}
+
+}  // namespace
+
+int main(int argc, char* argv[]) {
+  try {
+    if (argc < 2) throw std::runtime_error("Unknown option");
+    std::cout << "running " << argv[1] << " with arguments: ";
+    for (int i = 2; i < argc; ++i) std::cout << argv[i] << (i < argc - 1 ? ", " : "");
+    std::cout << '\n';
+    const std::string option(argv[1]);
+    const std::string out = argc > 2 && argv[2][0] ? argv[2] : ".";
+    const std::map<std::string, std::function<void()>> handlers = {
+        {"galaxy-sim-pm", [&] { galaxySimulationPM(out); }},
+        {"galaxy-sim-p3m", [&] { galaxySimulationP3M(out); }},
+        {"galaxy-collision-sim-pm", [&] { galaxyCollision(out, false); }},
+        {"galaxy-collision-sim-p3m", [&] { galaxyCollision(out, true); }},
+        {"cluster-sim-pm", [&] { plummer(out, false); }},
+        {"cluster-sim-p3m", [&] { plummer(out, true); }},
+        // galaxySimulationPMTiming / P3MTiming (source/demos.cpp:779-836, 953-1016): "n seconds"
+        {"galaxy-sim-pm-timing",
+         [&] {
+           for (int n = 10000; n <= 50000; n += 5000) galaxySimulationPM(out, n, 100, true);
+         }},
+        {"galaxy-sim-p3m-timing",
+         [&] {
+           for (int n = 10000; n <= 50000; n += 5000) galaxySimulationP3M(out, n, 25, true);
+         }},
+    };
+    const auto it = handlers.find(option);
+    if (it == handlers.end()) throw std::runtime_error("Unknown option: " + option);
+    it->second();
+  } catch (const std::exception& e) {
+    std::cerr << e.what() << '\n';
+    return 1;
+  }
+  return 0;
+}
