@@ -114,7 +114,7 @@ int sort_particles(pmgb_pm* h) {
   if (q) {
     rc = launch_chain_keys(h->pm[h->cur], h->vi[h->cur], n, q->cd, q->cfg.y_sorting, stop, h->keys, h->vals, h->st);
     if (rc) return rc;
-    const int bits = 32 + ilog2(q->ncells + 2);
+    const int bits = 32 + ilog2(q->nsub + 2);
     rc = radix_sort_pairs(&h->keys, &h->vals, &h->keys_alt, &h->vals_alt, h->hist, n, bits, h->st);
     if (rc) return rc;
     if (q->cfg.y_sorting) {
@@ -122,7 +122,7 @@ int sort_particles(pmgb_pm* h) {
       if (rc) return rc;
     }
     rc = launch_gather(h->keys, h->vals, n, h->pm[h->cur], h->vi[h->cur], h->pm[1 - h->cur],
-                       h->vi[1 - h->cur], q->cell_start, q->ncells + 1, stop, h->st);
+                       h->vi[1 - h->cur], q->cell_start, q->nsub + 1, stop, h->st);
     if (rc) return rc;
     h->cur = 1 - h->cur;
     return PMGB_OK;
@@ -183,7 +183,7 @@ int force(pmgb_pm* h, int kdk, float kick, int drift, int tag, bool timed) {
     if (rc) return rc;
   }
   // ev[4] is recorded just before the pair kernel (after its work-item setup)
-  rc = launch_pair(h->pm[h->cur], h->vi[h->cur], h->acc_pm, q->cell_start, q->cd.Mx, q->cd.My, q->cd.Mz,
+  rc = launch_pair(h->pm[h->cur], h->vi[h->cur], h->acc_pm, q->cell_start, q->cd,
                    q->item_cnt, q->item_off, q->nitems, q->items, q->counter, q->pp, q->table, sp,
                    kick, drift, kdk, h->pm[1 - h->cur], h->vi[1 - h->cur], h->acc,
                    q->count_pairs ? q->npairs : nullptr, stop,
@@ -588,6 +588,12 @@ int p3m_create_internal(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out,
   q->cd.HCy = (cfg->comp_box[1] / q->cd.My) / H;
   q->cd.HCz = (cfg->comp_box[2] / q->cd.Mz) / H;
   q->ncells = q->cd.Mx * q->cd.My * q->cd.Mz;
+  // 2 x 2 sub-columns per cell when the lists are y-sorted (the pair pass prunes by y window
+  // per sub-column); the reference's unsorted fill order keeps whole cells
+  q->cd.sub = cfg->y_sorting ? 2 : 1;
+  q->cd.HCsx = q->cd.HCx / q->cd.sub;
+  q->cd.HCsz = q->cd.HCz / q->cd.sub;
+  q->nsub = q->ncells * q->cd.sub * q->cd.sub;
   // initSRForceTable (source/p3mMethod.cpp:275-294) in the reference's float arithmetic
   const float re = cfg->cutoff / H, a = cfg->particle_diameter / H, eps = cfg->softening / H;
   q->delta2 = re * re / (500 - 1);
@@ -622,13 +628,14 @@ int p3m_create_internal(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out,
   q->pp.shape = cfg->cloud_shape;
   q->pp.a = a;
   q->pp.eps2 = eps * eps;
-  const size_t ntot = (size_t)q->ncells + 1;
+  const size_t ntot = (size_t)q->nsub + 1;  // sub-columns + the bucket outside the mesh
   int rc;
   if ((rc = dalloc(&q->cell_start, ntot + 1)) || (rc = dalloc(&q->item_cnt, ntot)) ||
       (rc = dalloc(&q->item_off, ntot)) || (rc = dalloc(&q->nitems, 1)) || (rc = dalloc(&q->counter, 1)) ||
-      // work items: 32-particle slices (pair counting, direct formula) or 64-particle slices x 27
-      // neighbours (the table pass), and its 27 partial-force slots per particle
-      (rc = dalloc(&q->items, 27 * ((size_t)pm->n / 64 + ntot) + (size_t)pm->n + 32)) ||
+      // slices of sub-columns (32 particles for pair counting / the direct formula, 64 for the
+      // table pass, which takes each slice once per neighbour cell), and the table pass's 27
+      // partial-force slots per particle
+      (rc = dalloc(&q->items, (size_t)pm->n / 32 + ntot + 32)) ||
       (rc = dalloc(&q->table, 500)) || (rc = dalloc(&q->npairs, 1)) ||
       (rc = dalloc(&q->slots, 27 * (size_t)std::max(pm->n, 1)))) {
     pmgb_p3m_destroy(q);
@@ -683,16 +690,37 @@ int pmgb_p3m_get_cell_lists(pmgb_p3m* q, int* order, int* counts, int* dims3) {
   if (!order && !counts) return PMGB_OK;
   pmgb_pm* h = q->pm;
   const int n = h->n;
-  std::vector<int> cs(q->ncells + 2);
-  std::vector<float4> hv(n);
+  const int sub2 = q->cd.sub * q->cd.sub;
+  std::vector<int> cs(q->nsub + 2);
+  std::vector<float4> hv(n), hp(n);
   PMGB_CUDA_TRY(cudaMemcpyAsync(cs.data(), q->cell_start, cs.size() * sizeof(int), cudaMemcpyDeviceToHost, h->st));
   PMGB_CUDA_TRY(cudaMemcpyAsync(hv.data(), h->vi[h->cur], n * sizeof(float4), cudaMemcpyDeviceToHost, h->st));
+  PMGB_CUDA_TRY(cudaMemcpyAsync(hp.data(), h->pm[h->cur], n * sizeof(float4), cudaMemcpyDeviceToHost, h->st));
   PMGB_CUDA_TRY(cudaStreamSynchronize(h->st));
   if (counts)
-    for (int c = 0; c < q->ncells; ++c) counts[c] = cs[c + 1] - cs[c];
+    for (int c = 0; c < q->ncells; ++c) counts[c] = cs[(c + 1) * sub2] - cs[c * sub2];
   if (order) {
-    const int inside = cs[q->ncells];
-    for (int k = 0; k < inside; ++k) std::memcpy(&order[k], &hv[k].w, 4);
+    // A cell's particles are stored sub-column by sub-column; the reference's list
+    // (fillWithYSorting) is the whole cell by ascending y, ties by index, which is the order of
+    // the device sort key (y as an order-preserving integer, -0 folded onto +0) then the id.
+    auto ykey = [](float y) {
+      uint32_t u;
+      std::memcpy(&u, &y, 4);
+      if (u == 0x80000000u) u = 0;
+      return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    };
+    std::vector<std::pair<uint64_t, int>> tmp;
+    int k = 0;
+    for (int c = 0; c < q->ncells; ++c) {
+      tmp.clear();
+      for (int s = cs[c * sub2]; s < cs[(c + 1) * sub2]; ++s) {
+        int id;
+        std::memcpy(&id, &hv[s].w, 4);
+        tmp.emplace_back(((uint64_t)ykey(hp[s].y) << 32) | (uint32_t)id, id);
+      }
+      if (q->cfg.y_sorting) std::sort(tmp.begin(), tmp.end());
+      for (auto& t : tmp) order[k++] = t.second;
+    }
   }
   return PMGB_OK;
 }

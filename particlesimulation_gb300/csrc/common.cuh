@@ -113,6 +113,11 @@ __device__ __forceinline__ void kick_drift(const StepParams& sp, float4& p, floa
 struct ChainDims {
   int Mx, My, Mz;
   float HCx, HCy, HCz;  // cell side, code units (lengthToCodeUnits(compBox/M, H))
+  // Sub-columns: each cell is split into sub x sub columns along x and z (the particles of a
+  // column sorted by y), so the pair pass can skip the columns of a neighbour cell that are out
+  // of reach in x and z.  sub = 1: plain cells.  Sub-column id = (cell * sub + sz) * sub + sx.
+  int sub;
+  float HCsx, HCsz;  // sub-column widths (HCx / sub, HCz / sub)
 };
 
 // Short-range pair pass parameters, code units.

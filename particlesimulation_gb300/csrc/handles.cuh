@@ -34,7 +34,7 @@ int launch_unpack(const float4* pm, const float4* vi, const float4* acc, int n, 
 int launch_pack(const float* pos, const float* vel, const float* mass_code, int n, float H,
                 float DT, int orig, float4* pm, float4* vi, cudaStream_t st);
 int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const int* cell_start,
-                int Mx, int My, int Mz, u32* item_cnt, u32* item_off, u32* nitems, int2* items,
+                const ChainDims& cd, u32* item_cnt, u32* item_off, u32* nitems, int2* items,
                 u32* counter, const PairParams& pp, const float* table, const StepParams& sp,
                 float kick, int drift, int kdk, float4* pm_out, float4* vi_out, float4* acc_out,
                 unsigned long long* npairs, int* stop, int num_sms, cudaEvent_t ev_pair,
@@ -86,7 +86,8 @@ struct pmgb_p3m {
   pmgb_p3m_config cfg{};
   pmgb::ChainDims cd{};
   int ncells = 0;
-  int* cell_start = nullptr;  // ncells + 2
+  int nsub = 0;               // sub-columns: ncells * cd.sub^2
+  int* cell_start = nullptr;  // nsub + 2: sub-column starts, the bucket outside the mesh, n
   pmgb::u32 *item_cnt = nullptr, *item_off = nullptr, *nitems = nullptr, *counter = nullptr;
   int2* items = nullptr;
   float* table = nullptr;

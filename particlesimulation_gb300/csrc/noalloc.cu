@@ -128,6 +128,7 @@ extern "C" int pmgb_chaining_mesh_fill_noalloc(const float* d_pos, int n,
                      " outside [0, " + std::to_string(kNoAllocMaxParticles) + "]"),
            PMGB_EINVAL;
   ChainDims c;
+  c.sub = 1;
   c.Mx = (int)(cfg->comp_box[0] / cfg->cutoff);
   c.My = (int)(cfg->comp_box[1] / cfg->cutoff);
   c.Mz = (int)(cfg->comp_box[2] / cfg->cutoff);

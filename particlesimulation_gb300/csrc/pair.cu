@@ -31,6 +31,8 @@ namespace pmgb {
 struct ChainDimsP {
   int Mx, My, Mz;
   int ncells;
+  int sub;            // sub-columns per cell along x and z
+  float HCsx, HCsz;   // sub-column widths
 };
 
 constexpr int PAIR_THREADS = 256;
@@ -114,15 +116,16 @@ __global__ void __launch_bounds__(PAIR_THREADS) pair_kernel(
     it = __shfl_sync(0xFFFFFFFFu, it, 0);
     if (it >= nitems) break;
     const int2 item = items[it];
-    const int cell = item.x;
-    const int cend = cell_start[cell + 1];
+    const int sub2 = cd.sub * cd.sub;
+    const int cell = item.x / sub2;
+    const int cend = cell_start[item.x + 1];
     const int i = item.y + lane;
     const bool valid = i < cend;
     const int last = min(item.y + 31, cend - 1);
     const float4 pi = pm[valid ? i : last];
     float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
 
-    if (cell < cd.ncells) {
+    if (cell < cd.ncells) for (int qs = 0; qs < sub2; ++qs) {
       const int gx = cell % cd.Mx, gy = (cell / cd.Mx) % cd.My, gz = cell / (cd.Mx * cd.My);
       // y range of the slice: lane 0 holds its first particle, lane 31 its last (lanes past
       // the end of the cell load the last particle)
@@ -133,7 +136,7 @@ __global__ void __launch_bounds__(PAIR_THREADS) pair_kernel(
       if (lane < 27) {
         const int nx = gx + lane % 3 - 1, ny = gy + (lane / 3) % 3 - 1, nz = gz + lane / 9 - 1;
         if (nx >= 0 && ny >= 0 && nz >= 0 && nx < cd.Mx && ny < cd.My && nz < cd.Mz) {
-          const int cn = nx + ny * cd.Mx + nz * cd.Mx * cd.My;
+          const int cn = (nx + ny * cd.Mx + nz * cd.Mx * cd.My) * sub2 + qs;
           jb = cell_start[cn];
           je = cell_start[cn + 1];
           if (pp.ysort && je > jb) {
@@ -315,17 +318,21 @@ __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const float2* tab = tab_all + (lane & (SLOT_REP - 1));
-  const u32 nitems = *nitems_p;
+  const u32 nitems = *nitems_p * NNB;  // every slice once per neighbour cell
   const float inv_d2 = pp.inv_d2;
+  const int sub = cd.sub, sub2 = sub * sub;
+  // a neighbour sub-column is skipped when its x-z distance from the slice's sub-column is at
+  // least the cutoff (with a margin far above the rounding of the sub-column assignment)
+  const float gap_margin = 1e-3f * fminf(cd.HCsx, cd.HCsz);
   for (;;) {
     u32 it = 0;
     if (lane == 0) it = atomicAdd(counter, 1u);
     it = __shfl_sync(0xFFFFFFFFu, it, 0);
     if (it >= nitems) break;
-    const int2 item = items[it];
-    const int cell = item.x / NNB;
-    const int k = item.x - cell * NNB;
-    const int cend = cell_start[cell + 1];
+    const int2 item = items[it / NNB];
+    const int k = (int)(it % NNB);
+    const int cell = item.x / sub2;
+    const int cend = cell_start[item.x + 1];
     const int last = min(item.y + SLOT_SLICE - 1, cend - 1);
     SlotI I[SLOT_IPL];
 #pragma unroll
@@ -337,14 +344,23 @@ __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
     if (cell < cd.ncells) {
       const int gx = cell % cd.Mx, gy = (cell / cd.Mx) % cd.My, gz = cell / (cd.Mx * cd.My);
       const int nx = gx + k % 3 - 1, ny = gy + (k / 3) % 3 - 1, nz = gz + k / 9 - 1;
-      if (nx >= 0 && ny >= 0 && nz >= 0 && nx < cd.Mx && ny < cd.My && nz < cd.Mz) {
-        const int cn = nx + ny * cd.Mx + nz * cd.Mx * cd.My;
+      // the slice's sub-column: x and z ranges in code units
+      const int isx = item.x % sub, isz = (item.x / sub) % sub;
+      const float ix0 = (gx * sub + isx) * cd.HCsx, iz0 = (gz * sub + isz) * cd.HCsz;
+      // y range of the slice: its first particle (lane 0, u = 0) and its last one
+      const float ylo = __shfl_sync(0xFFFFFFFFu, I[0].p.y, 0) - pp.re;
+      const float yhi = __ldg(&pm[last].y) + pp.re;
+      if (nx >= 0 && ny >= 0 && nz >= 0 && nx < cd.Mx && ny < cd.My && nz < cd.Mz)
+      for (int qs = 0; qs < sub2; ++qs) {
+        const int jsx = qs % sub, jsz = qs / sub;
+        const float jx0 = (nx * sub + jsx) * cd.HCsx, jz0 = (nz * sub + jsz) * cd.HCsz;
+        const float gxs = fmaxf(fmaxf(jx0 - (ix0 + cd.HCsx), ix0 - (jx0 + cd.HCsx)) - gap_margin, 0.f);
+        const float gzs = fmaxf(fmaxf(jz0 - (iz0 + cd.HCsz), iz0 - (jz0 + cd.HCsz)) - gap_margin, 0.f);
+        if (gxs * gxs + gzs * gzs >= pp.re2) continue;
+        const int cn = (nx + ny * cd.Mx + nz * cd.Mx * cd.My) * sub2 + qs;
         int b = cell_start[cn];
         int e = cell_start[cn + 1];
         if (pp.ysort && e > b) {
-          // y range of the slice: its first particle (lane 0, u = 0) and its last one
-          const float ylo = __shfl_sync(0xFFFFFFFFu, I[0].p.y, 0) - pp.re;
-          const float yhi = __ldg(&pm[last].y) + pp.re;
           b = warp_y_bound<false>(pm, b, e, ylo, lane);
           e = warp_y_bound<true>(pm, b, e, yhi, lane);
         }
@@ -409,51 +425,48 @@ __global__ void __launch_bounds__(256) pair_epilogue_kernel(
 }
 
 // ------------------------------------------------------------------ work items ---------
-// per_slice = 1: one item (cell, slice start) per 32-particle slice; per_slice = 27: items
-// (cell * 27 + k, slice start) per 64-particle slice and neighbour k.
+// One item (sub-column id, slice start) per slice of `slice` particles of a sub-column; the
+// table pass takes each item once per neighbour cell (item index * 27 + k).
 __global__ void item_count_kernel(const int* __restrict__ cell_start, int ncells_total,
-                                  u32* __restrict__ cnt, int slice, int per_slice, const int* stop) {
+                                  u32* __restrict__ cnt, int slice, const int* stop) {
   if (*stop) return;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells_total) return;
   const int n = cell_start[c + 1] - cell_start[c];
-  cnt[c] = (u32)((n + slice - 1) / slice) * (u32)per_slice;
+  cnt[c] = (u32)((n + slice - 1) / slice);
 }
 
 __global__ void item_build_kernel(const int* __restrict__ cell_start, const u32* __restrict__ off,
                                   int ncells_total, int2* __restrict__ items, int slice,
-                                  int per_slice, const int* stop) {
+                                  const int* stop) {
   if (*stop) return;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells_total) return;
   const int b = cell_start[c], e = cell_start[c + 1];
   u32 o = off[c];
-  for (int s = b; s < e; s += slice)
-    for (int k = 0; k < per_slice; ++k) items[o++] = make_int2(c * per_slice + k, s);
+  for (int s = b; s < e; s += slice) items[o++] = make_int2(c, s);
 }
 
 int exclusive_scan(const u32* in, u32* out, int n, u32* total, cudaStream_t st);
 
 int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const int* cell_start,
-                int Mx, int My, int Mz, u32* item_cnt, u32* item_off, u32* nitems, int2* items,
+                const ChainDims& chd, u32* item_cnt, u32* item_off, u32* nitems, int2* items,
                 u32* counter, const PairParams& pp, const float* table, const StepParams& sp,
                 float kick, int drift, int kdk, float4* pm_out, float4* vi_out, float4* acc_out,
                 unsigned long long* npairs, int* stop, int num_sms, cudaEvent_t ev_pair,
                 cudaStream_t st, int equal_mass, float4* slots, int n) {
-  const int ncells = Mx * My * Mz;
-  const int ntot = ncells + 1;  // + the bucket of particles outside the chaining mesh
+  const int ncells = chd.Mx * chd.My * chd.Mz;
+  const int ntot = ncells * chd.sub * chd.sub + 1;  // sub-columns + the bucket outside the mesh
   const bool slotted = pp.use_table && !npairs && slots;
   const int slice = slotted ? SLOT_SLICE : 32;
-  const int per_slice = slotted ? NNB : 1;
-  item_count_kernel<<<(ntot + 255) / 256, 256, 0, st>>>(cell_start, ntot, item_cnt, slice, per_slice, stop);
+  item_count_kernel<<<(ntot + 255) / 256, 256, 0, st>>>(cell_start, ntot, item_cnt, slice, stop);
   int rc = exclusive_scan(item_cnt, item_off, ntot, nitems, st);
   if (rc) return rc;
-  item_build_kernel<<<(ntot + 255) / 256, 256, 0, st>>>(cell_start, item_off, ntot, items, slice,
-                                                        per_slice, stop);
+  item_build_kernel<<<(ntot + 255) / 256, 256, 0, st>>>(cell_start, item_off, ntot, items, slice, stop);
   PMGB_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(u32), st));
   if (npairs) PMGB_CUDA_TRY(cudaMemsetAsync(npairs, 0, sizeof(unsigned long long), st));
   if (ev_pair) PMGB_CUDA_TRY(cudaEventRecord(ev_pair, st));
-  ChainDimsP cd{Mx, My, Mz, ncells};
+  ChainDimsP cd{chd.Mx, chd.My, chd.Mz, ncells, chd.sub, chd.HCsx, chd.HCsz};
   const dim3 grid(num_sms * 8), block(PAIR_THREADS);
   if (slotted) {  // 64 KB + staging of dynamic shared memory (set for the current device)
     PMGB_CUDA_TRY(cudaFuncSetAttribute(pair_slot_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SLOT_SMEM));

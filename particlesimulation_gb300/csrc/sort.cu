@@ -177,7 +177,15 @@ __global__ void chain_keys_kernel(const float4* __restrict__ pm, const float4* _
   if (i >= n) return;
   float4 p = pm[i];
   int cell = chain_cell(c, p.x, p.y, p.z);
-  if (cell < 0) cell = ncells;  // outside the chaining mesh: last bucket, no pair forces
+  const int sub2 = c.sub * c.sub;
+  if (cell < 0) {
+    cell = ncells * sub2;  // outside the chaining mesh: last bucket, no pair forces
+  } else if (c.sub > 1) {  // sub-column of the cell (clamped: x / HCs and x / HC round apart)
+    const int cx = cell % c.Mx, cz = cell / (c.Mx * c.My);
+    const int sx = min(max((int)__fdiv_rn(p.x, c.HCsx) - cx * c.sub, 0), c.sub - 1);
+    const int sz = min(max((int)__fdiv_rn(p.z, c.HCsz) - cz * c.sub, 0), c.sub - 1);
+    cell = (cell * c.sub + sz) * c.sub + sx;
+  }
   u32 lo;
   if (ysort) {
     lo = float_key(p.y);
@@ -266,7 +274,7 @@ __global__ void fill_int_kernel(int* p, int n, int v) {
 // ------------------------------------------------------------------ host side ---------
 int launch_chain_keys(const float4* pm, const float4* vi, int n, ChainDims c, int ysort,
                       const int* stop, u64* keys, u32* vals, cudaStream_t st) {
-  int ncells = c.Mx * c.My * c.Mz;
+  int ncells = c.Mx * c.My * c.Mz;  // keys hold sub-column ids (cells x sub^2, then the bucket)
   chain_keys_kernel<<<(n + 255) / 256, 256, 0, st>>>(pm, vi, n, c, ysort, ncells, stop, keys, vals);
   PMGB_LAUNCH_CHECK();
   count_launches(1);
