@@ -60,6 +60,10 @@ def parse():
     ap.add_argument("--closure-bound", type=float, default=0.05,
                     help="judge bound: median relative deviation from plain P3M")
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--profile-closure", type=int, default=0, metavar="K",
+                    help="only run K learned-closure steps on the 1,048,576-particle disk (untrained "
+                         "weights: same work) and print the stage times (the command profiled "
+                         "with ncu)")
     ap.add_argument("--profile-forces", type=int, default=0, metavar="K",
                     help="only run K force evaluations of the workload and print the stage "
                          "times (the command profiled with ncu)")
@@ -80,6 +84,22 @@ def run_profile_forces(args):
         p3m.close()
     pm.close()
     print(json.dumps(out))
+
+
+def run_profile_closure(args):
+    import particlesimulation_gb300 as P
+    from particlesimulation_gb300 import workloads as W
+    w = W.disk_p3m_1m()
+    pm, _ = make_system(W.Workload(**{**w.__dict__, "p3m": None}))
+    q = w.p3m
+    cl = P.LearnedClosure(pm, q["comp_box"], q["cutoff"], q["diameter"], q["softening"],
+                          P.CloudShape(q["cloud_shape"]), 0.5 * q["cutoff"], seed=args.seed)
+    cl.setMode(cl.LEARNED)
+    pm.run(0)
+    _, _, ms = pm.advance(args.profile_closure)
+    print(json.dumps({"learned_ms_per_step": ms / max(args.profile_closure, 1)}))
+    cl.close()
+    pm.close()
 
 
 def dist_env():
@@ -573,7 +593,9 @@ def run_reference(args):
 
 def main():
     args = parse()
-    if args.profile_forces:
+    if args.profile_closure:
+        run_profile_closure(args)
+    elif args.profile_forces:
         run_profile_forces(args)
     elif args.impl == "reference":
         run_reference(args)

@@ -10,32 +10,35 @@ __device__ __forceinline__ float phi_at(const float* __restrict__ phi, const Mes
   return __ldg(&phi[((size_t)wrapi(z, m.nz) * m.ny + wrapi(y, m.ny)) * m.nx + wrapi(x, m.nx)]);
 }
 
-template <int FDS>
-__device__ __forceinline__ float3 field_at(const float* __restrict__ phi, const MeshDims& m, int x,
-                                           int y, int z) {
+// Where the potential is read: the mesh in global memory, indices wrapped periodically as in
+// Grid::getPotential (reference source/grid.cpp:66-68).
+struct PhiGlobal {
+  const float* __restrict__ phi;
+  MeshDims m;
+  __device__ __forceinline__ float operator()(int x, int y, int z) const { return phi_at(phi, m, x, y, z); }
+};
+
+template <int FDS, class Phi>
+__device__ __forceinline__ float3 field_at(const Phi& phi_at, int x, int y, int z) {
   float3 f;
   if (FDS == 0) {
-    f.x = -0.5f * (phi_at(phi, m, x + 1, y, z) - phi_at(phi, m, x - 1, y, z));
-    f.y = -0.5f * (phi_at(phi, m, x, y + 1, z) - phi_at(phi, m, x, y - 1, z));
-    f.z = -0.5f * (phi_at(phi, m, x, y, z + 1) - phi_at(phi, m, x, y, z - 1));
+    f.x = -0.5f * (phi_at(x + 1, y, z) - phi_at(x - 1, y, z));
+    f.y = -0.5f * (phi_at(x, y + 1, z) - phi_at(x, y - 1, z));
+    f.z = -0.5f * (phi_at(x, y, z + 1) - phi_at(x, y, z - 1));
   } else {
     const float c = -1.0f / 12;
-    f.x = c * (-phi_at(phi, m, x + 2, y, z) + 8 * phi_at(phi, m, x + 1, y, z) -
-               8 * phi_at(phi, m, x - 1, y, z) + phi_at(phi, m, x - 2, y, z));
-    f.y = c * (-phi_at(phi, m, x, y + 2, z) + 8 * phi_at(phi, m, x, y + 1, z) -
-               8 * phi_at(phi, m, x, y - 1, z) + phi_at(phi, m, x, y - 2, z));
-    f.z = c * (-phi_at(phi, m, x, y, z + 2) + 8 * phi_at(phi, m, x, y, z + 1) -
-               8 * phi_at(phi, m, x, y, z - 1) + phi_at(phi, m, x, y, z - 2));
+    f.x = c * (-phi_at(x + 2, y, z) + 8 * phi_at(x + 1, y, z) - 8 * phi_at(x - 1, y, z) + phi_at(x - 2, y, z));
+    f.y = c * (-phi_at(x, y + 2, z) + 8 * phi_at(x, y + 1, z) - 8 * phi_at(x, y - 1, z) + phi_at(x, y - 2, z));
+    f.z = c * (-phi_at(x, y, z + 2) + 8 * phi_at(x, y, z + 1) - 8 * phi_at(x, y, z - 1) + phi_at(x, y, z - 2));
   }
   return f;
 }
 
-template <int IS, int FDS>
-__device__ __forceinline__ float3 interpolate(const float* __restrict__ phi, const MeshDims& m,
-                                              float x, float y, float z) {
+template <int IS, int FDS, class Phi>
+__device__ __forceinline__ float3 interpolate(const Phi& phi, float x, float y, float z) {
   float3 r = make_float3(0.f, 0.f, 0.f);
   if (IS == 0) {
-    return field_at<FDS>(phi, m, (int)roundf(x), (int)roundf(y), (int)roundf(z));
+    return field_at<FDS>(phi, (int)roundf(x), (int)roundf(y), (int)roundf(z));
   } else if (IS == 1) {
     const int xi = (int)x, yi = (int)y, zi = (int)z;
     const float dx = x - xi, dy = y - yi, dz = z - zi;
@@ -46,7 +49,7 @@ __device__ __forceinline__ float3 interpolate(const float* __restrict__ phi, con
               oz[8] = {0, 0, 0, 1, 0, 1, 1, 1};
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
-      float3 f = field_at<FDS>(phi, m, xi + ox[c], yi + oy[c], zi + oz[c]);
+      float3 f = field_at<FDS>(phi, xi + ox[c], yi + oy[c], zi + oz[c]);
       r.x += w[c] * f.x;
       r.y += w[c] * f.y;
       r.z += w[c] * f.z;
@@ -63,7 +66,7 @@ __device__ __forceinline__ float3 interpolate(const float* __restrict__ phi, con
 #pragma unroll
         for (int t3 = -1; t3 <= 1; ++t3) {
           const float w = 0.125f * (T2 * tsc_w(dz, t3));
-          float3 f = field_at<FDS>(phi, m, xi + t1, yi + t2, zi + t3);
+          float3 f = field_at<FDS>(phi, xi + t1, yi + t2, zi + t3);
           r.x += w * f.x;
           r.y += w * f.y;
           r.z += w * f.z;
@@ -89,13 +92,12 @@ __device__ __forceinline__ float3 external_field(const StepParams& sp, float x, 
 
 
 // One particle: interpolated field + external field -> acc[i]; with KDK also kick / drift.
-template <int IS, int FDS, bool KDK>
-__device__ __forceinline__ void interp_particle(float4* __restrict__ pm, float4* __restrict__ vi,
-                                                float4* __restrict__ acc, int i,
-                                                const float* __restrict__ phi, const StepParams& sp,
-                                                float kick, int drift, int* stop) {
-  float4 p = pm[i];
-  float3 a = interpolate<IS, FDS>(phi, sp.m, p.x, p.y, p.z);
+template <int IS, int FDS, bool KDK, class Phi>
+__device__ __forceinline__ void interp_particle_p(float4* __restrict__ pm, float4* __restrict__ vi,
+                                                  float4* __restrict__ acc, int i, float4 p,
+                                                  const Phi& phi, const StepParams& sp, float kick,
+                                                  int drift, int* stop) {
+  float3 a = interpolate<IS, FDS>(phi, p.x, p.y, p.z);
   const float3 e = external_field(sp, p.x, p.y, p.z);
   a.x += e.x;
   a.y += e.y;
@@ -107,6 +109,14 @@ __device__ __forceinline__ void interp_particle(float4* __restrict__ pm, float4*
     pm[i] = p;
     vi[i] = v;
   }
+}
+
+template <int IS, int FDS, bool KDK>
+__device__ __forceinline__ void interp_particle(float4* __restrict__ pm, float4* __restrict__ vi,
+                                                float4* __restrict__ acc, int i,
+                                                const float* __restrict__ phi, const StepParams& sp,
+                                                float kick, int drift, int* stop) {
+  interp_particle_p<IS, FDS, KDK>(pm, vi, acc, i, pm[i], PhiGlobal{phi, sp.m}, sp, kick, drift, stop);
 }
 
 }  // namespace pmgb

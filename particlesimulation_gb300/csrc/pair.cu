@@ -348,21 +348,26 @@ __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
       const int isx = item.x % sub, isz = (item.x / sub) % sub;
       const float ix0 = (gx * sub + isx) * cd.HCsx, iz0 = (gz * sub + isz) * cd.HCsz;
       // y range of the slice: its first particle (lane 0, u = 0) and its last one
-      const float ylo = __shfl_sync(0xFFFFFFFFu, I[0].p.y, 0) - pp.re;
-      const float yhi = __ldg(&pm[last].y) + pp.re;
+      const float ys0 = __shfl_sync(0xFFFFFFFFu, I[0].p.y, 0);
+      const float ys1 = __ldg(&pm[last].y);
       if (nx >= 0 && ny >= 0 && nz >= 0 && nx < cd.Mx && ny < cd.My && nz < cd.Mz)
       for (int qs = 0; qs < sub2; ++qs) {
         const int jsx = qs % sub, jsz = qs / sub;
         const float jx0 = (nx * sub + jsx) * cd.HCsx, jz0 = (nz * sub + jsz) * cd.HCsz;
         const float gxs = fmaxf(fmaxf(jx0 - (ix0 + cd.HCsx), ix0 - (jx0 + cd.HCsx)) - gap_margin, 0.f);
         const float gzs = fmaxf(fmaxf(jz0 - (iz0 + cd.HCsz), iz0 - (jz0 + cd.HCsz)) - gap_margin, 0.f);
-        if (gxs * gxs + gzs * gzs >= pp.re2) continue;
+        const float g2 = gxs * gxs + gzs * gzs;
+        if (g2 >= pp.re2) continue;
+        // a pair in range has |dy|^2 < re^2 - (its x-z distance)^2 <= re^2 - g2: the y window
+        // of this sub-column is the chord of the cutoff sphere at the sub-column's x-z gap, widened
+        // by 1e-5 of the coordinates' size against float rounding of the comparisons
+        const float h = sqrtf(pp.re2 - g2) + 1e-5f * (1.f + fabsf(ys1));
         const int cn = (nx + ny * cd.Mx + nz * cd.Mx * cd.My) * sub2 + qs;
         int b = cell_start[cn];
         int e = cell_start[cn + 1];
         if (pp.ysort && e > b) {
-          b = warp_y_bound<false>(pm, b, e, ylo, lane);
-          e = warp_y_bound<true>(pm, b, e, yhi, lane);
+          b = warp_y_bound<false>(pm, b, e, ys0 - h, lane);
+          e = warp_y_bound<true>(pm, b, e, ys1 + h, lane);
         }
         for (int j0 = b; j0 < e; j0 += 32) {
           const int jj = j0 + lane;
