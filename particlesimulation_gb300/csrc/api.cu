@@ -184,7 +184,7 @@ int force(pmgb_pm* h, int kdk, float kick, int drift, int tag, bool timed) {
   }
   // ev[4] is recorded just before the pair kernel (after its work-item setup)
   rc = launch_pair(h->pm[h->cur], h->vi[h->cur], h->acc_pm, q->cell_start, q->cd,
-                   q->item_cnt, q->item_off, q->nitems, q->items, q->counter, q->pp, q->table, sp,
+                   q->item_cnt, q->item_off, q->scan_tmp, q->nitems, q->items, q->counter, q->pp, q->table, sp,
                    kick, drift, kdk, h->pm[1 - h->cur], h->vi[1 - h->cur], h->acc,
                    q->count_pairs ? q->npairs : nullptr, stop,
                    h->num_sms, timed ? h->ev[4] : nullptr, h->st, h->equal_mass, q->slots, n);
@@ -305,7 +305,7 @@ int pmgb_pm_create(const pmgb_pm_config* cfg, int n, const float* state, const f
   if ((rc = dalloc(&h->pm[0], N)) || (rc = dalloc(&h->pm[1], N)) || (rc = dalloc(&h->vi[0], N)) ||
       (rc = dalloc(&h->vi[1], N)) || (rc = dalloc(&h->acc, N)) || (rc = dalloc(&h->acc_pm, N)) ||
       (rc = dalloc(&h->keys, N)) || (rc = dalloc(&h->keys_alt, N)) || (rc = dalloc(&h->vals, N)) ||
-      (rc = dalloc(&h->vals_alt, N)) || (rc = dalloc(&h->hist, (size_t)256 * radix_hist_blocks((int)N))) ||
+      (rc = dalloc(&h->vals_alt, N)) || (rc = dalloc(&h->hist, radix_hist_words((int)N))) ||
       (rc = dalloc(&h->rho, (size_t)m.L)) || (rc = dalloc(&h->spec, half)) || (rc = dalloc(&h->phi, (size_t)m.L)) ||
       (rc = dalloc(&h->ghat, half)) || (rc = dalloc(&h->tw, (size_t)h->nmax / 2 + 1)) || (rc = dalloc(&h->flags, 4)) ||
       (rc = dalloc(&h->stage, 9 * N)) || (rc = dalloc(&h->mass_code, N)))
@@ -632,6 +632,7 @@ int p3m_create_internal(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out,
   int rc;
   if ((rc = dalloc(&q->cell_start, ntot + 1)) || (rc = dalloc(&q->item_cnt, ntot)) ||
       (rc = dalloc(&q->item_off, ntot)) || (rc = dalloc(&q->nitems, 1)) || (rc = dalloc(&q->counter, 1)) ||
+      (rc = dalloc(&q->scan_tmp, (size_t)scan_scratch_words((int)ntot))) ||
       // slices of sub-columns (32 particles for pair counting / the direct formula, 64 for the
       // table pass, which takes each slice once per neighbour cell), and the table pass's 27
       // partial-force slots per particle
@@ -662,8 +663,8 @@ int pmgb_p3m_destroy(pmgb_p3m* q) {
     if (q->pm->p3m == q) q->pm->p3m = nullptr;
     q->pm->since_sort = 1 << 30;
   }
-  void* ptrs[] = {q->cell_start, q->item_cnt, q->item_off, q->nitems, q->counter, q->items, q->table, q->npairs,
-                  q->slots};
+  void* ptrs[] = {q->cell_start, q->item_cnt, q->item_off, q->scan_tmp, q->nitems, q->counter, q->items, q->table,
+                  q->npairs, q->slots};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete q;

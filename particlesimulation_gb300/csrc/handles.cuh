@@ -6,9 +6,11 @@
 namespace pmgb {
 
 int radix_hist_blocks(int n);
+size_t radix_hist_words(int n);  // size of radix_sort_pairs' hist buffer
 int radix_sort_pairs(u64** keys, u32** vals, u64** keys_alt, u32** vals_alt, u32* hist, int n,
                      int nbits, cudaStream_t st);
-int exclusive_scan(const u32* in, u32* out, int n, u32* total, cudaStream_t st);
+int scan_scratch_words(int n);   // size of exclusive_scan's scratch buffer
+int exclusive_scan(const u32* in, u32* out, int n, u32* total, u32* scratch, cudaStream_t st);
 int launch_chain_keys(const float4* pm, const float4* vi, int n, ChainDims c, int ysort,
                       const int* stop, u64* keys, u32* vals, cudaStream_t st);
 int launch_fix_ties(const u64* keys, u32* vals, const float4* vi, int n, const int* stop,
@@ -34,7 +36,7 @@ int launch_unpack(const float4* pm, const float4* vi, const float4* acc, int n, 
 int launch_pack(const float* pos, const float* vel, const float* mass_code, int n, float H,
                 float DT, int orig, float4* pm, float4* vi, cudaStream_t st);
 int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const int* cell_start,
-                const ChainDims& cd, u32* item_cnt, u32* item_off, u32* nitems, int2* items,
+                const ChainDims& cd, u32* item_cnt, u32* item_off, u32* scan_tmp, u32* nitems, int2* items,
                 u32* counter, const PairParams& pp, const float* table, const StepParams& sp,
                 float kick, int drift, int kdk, float4* pm_out, float4* vi_out, float4* acc_out,
                 unsigned long long* npairs, int* stop, int num_sms, cudaEvent_t ev_pair,
@@ -89,6 +91,7 @@ struct pmgb_p3m {
   int nsub = 0;               // sub-columns: ncells * cd.sub^2
   int* cell_start = nullptr;  // nsub + 2: sub-column starts, the bucket outside the mesh, n
   pmgb::u32 *item_cnt = nullptr, *item_off = nullptr, *nitems = nullptr, *counter = nullptr;
+  pmgb::u32* scan_tmp = nullptr;  // scratch of the item-count scan (scan_scratch_words)
   int2* items = nullptr;
   float* table = nullptr;
   float table_h[500];

@@ -30,7 +30,7 @@ constexpr int kNoAllocHistBlocks = (kNoAllocMaxParticles + 4095) / 4096;  // rad
 
 static __device__ __align__(256) u64 g_na_keys[2][kNoAllocMaxParticles];
 static __device__ __align__(256) u32 g_na_vals[2][kNoAllocMaxParticles];
-static __device__ __align__(256) u32 g_na_hist[256 * kNoAllocHistBlocks];
+static __device__ __align__(256) u32 g_na_hist[256 * kNoAllocHistBlocks + 256];  // + row totals
 static __device__ __align__(256) int g_na_cell_start[kNoAllocMaxCells + 2];
 
 int radix_hist_blocks(int n);

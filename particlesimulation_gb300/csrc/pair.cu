@@ -452,10 +452,10 @@ __global__ void item_build_kernel(const int* __restrict__ cell_start, const u32*
   for (int s = b; s < e; s += slice) items[o++] = make_int2(c, s);
 }
 
-int exclusive_scan(const u32* in, u32* out, int n, u32* total, cudaStream_t st);
+int exclusive_scan(const u32* in, u32* out, int n, u32* total, u32* scratch, cudaStream_t st);
 
 int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const int* cell_start,
-                const ChainDims& chd, u32* item_cnt, u32* item_off, u32* nitems, int2* items,
+                const ChainDims& chd, u32* item_cnt, u32* item_off, u32* scan_tmp, u32* nitems, int2* items,
                 u32* counter, const PairParams& pp, const float* table, const StepParams& sp,
                 float kick, int drift, int kdk, float4* pm_out, float4* vi_out, float4* acc_out,
                 unsigned long long* npairs, int* stop, int num_sms, cudaEvent_t ev_pair,
@@ -465,7 +465,7 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
   const bool slotted = pp.use_table && !npairs && slots;
   const int slice = slotted ? SLOT_SLICE : 32;
   item_count_kernel<<<(ntot + 255) / 256, 256, 0, st>>>(cell_start, ntot, item_cnt, slice, stop);
-  int rc = exclusive_scan(item_cnt, item_off, ntot, nitems, st);
+  int rc = exclusive_scan(item_cnt, item_off, ntot, nitems, scan_tmp, st);
   if (rc) return rc;
   item_build_kernel<<<(ntot + 255) / 256, 256, 0, st>>>(cell_start, item_off, ntot, items, slice, stop);
   PMGB_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(u32), st));

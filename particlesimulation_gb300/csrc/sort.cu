@@ -10,8 +10,9 @@
 //   * PM: Morton order of 4x4x4-cell bricks, for deposit / interpolation locality only (the
 //     density is computed in integer arithmetic, so results do not depend on the order).
 //
-// The radix sort is our own: per pass a block histogram, one exclusive scan, and a stable
-// scatter that ranks keys inside a warp with __match_any_sync.
+// The radix sort is our own: per pass a block histogram, a scan of each digit's row of block
+// counts (one CTA per digit), and a stable scatter that ranks keys inside a warp with
+// __match_any_sync.
 #include "common.cuh"
 
 namespace pmgb {
@@ -46,43 +47,127 @@ __global__ void __launch_bounds__(RS_THREADS) rs_hist_kernel(const u64* __restri
   for (int d = threadIdx.x; d <= (int)mask; d += RS_THREADS) hist[d * nblocks + blockIdx.x] = h[d];
 }
 
-// Single-CTA exclusive scan (in place allowed).  Used for the radix histograms (256 x blocks)
-// and for small count arrays.
-__global__ void __launch_bounds__(1024) exclusive_scan_kernel(const u32* __restrict__ in,
-                                                              u32* __restrict__ out, int n,
-                                                              u32* __restrict__ total) {
-  __shared__ u32 s[1024];
-  const int t = threadIdx.x;
-  const int chunk = (n + 1023) / 1024;
-  const int b = t * chunk, e = min(n, b + chunk);
-  u32 sum = 0;
-  for (int i = b; i < e; ++i) sum += in[i];
-  s[t] = sum;
-  __syncthreads();
-  for (int off = 1; off < 1024; off <<= 1) {
-    u32 v = t >= off ? s[t - off] : 0;
-    __syncthreads();
-    s[t] += v;
-    __syncthreads();
+// ------------------------------------------------------------------ scans --------------
+// Exclusive scans of u32 arrays.  One 256-thread CTA scans a tile of SCAN_TILE = 4096 values:
+// each warp owns 512 consecutive values, reads them in 16 coalesced rounds of 32 and scans each
+// round with shuffles, starting from the sum of the warps before it.
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_WARPS = SCAN_THREADS / 32;
+constexpr int SCAN_ROUNDS = 16;
+constexpr int SCAN_TILE = SCAN_WARPS * SCAN_ROUNDS * 32;
+
+__device__ __forceinline__ u32 warp_incl_scan(u32 v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const u32 t = __shfl_up_sync(0xFFFFFFFFu, v, o);
+    if (lane >= o) v += t;
   }
-  u32 run = s[t] - sum;
-  for (int i = b; i < e; ++i) {
-    u32 v = in[i];
-    out[i] = run;
-    run += v;
-  }
-  if (total && t == 1023) *total = s[1023];
+  return v;
 }
 
+// out[i] = carry + in[0] + ... + in[i-1] for i < len (len <= SCAN_TILE; in == out allowed: every
+// value is read before the CTA's first write).  Returns the sum of in[0, len) to every thread.
+// ws: SCAN_WARPS words of shared memory.  Called by all threads of the CTA.
+__device__ u32 tile_scan(const u32* in, u32* out, int len, u32 carry, u32* ws) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int wb = warp * (SCAN_ROUNDS * 32);
+  u32 v[SCAN_ROUNDS];
+  u32 s = 0;
+#pragma unroll
+  for (int r = 0; r < SCAN_ROUNDS; ++r) {
+    const int i = wb + r * 32 + lane;
+    v[r] = i < len ? in[i] : 0u;
+    s += v[r];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
+  if (lane == 0) ws[warp] = s;
+  __syncthreads();
+  u32 base = carry, tot = 0;
+#pragma unroll
+  for (int w = 0; w < SCAN_WARPS; ++w) {
+    const u32 t = ws[w];
+    base += w < warp ? t : 0u;
+    tot += t;
+  }
+  __syncthreads();  // ws may be reused by the caller's next tile
+#pragma unroll
+  for (int r = 0; r < SCAN_ROUNDS; ++r) {
+    const u32 x = warp_incl_scan(v[r], lane);
+    const int i = wb + r * 32 + lane;
+    if (i < len) out[i] = base + x - v[r];
+    base += __shfl_sync(0xFFFFFFFFu, x, 31);
+  }
+  return tot;
+}
+
+// One CTA scans all of in[0, n), tile after tile; total (if given) = the sum.
+__global__ void __launch_bounds__(SCAN_THREADS) scan_serial_kernel(const u32* in, u32* out, int n,
+                                                                   u32* total) {
+  __shared__ u32 ws[SCAN_WARPS];
+  u32 carry = 0;
+  for (int b = 0; b < n; b += SCAN_TILE) carry += tile_scan(in + b, out + b, min(SCAN_TILE, n - b), carry, ws);
+  if (total && threadIdx.x == 0) *total = carry;
+}
+
+// partial[t] = sum of tile t.
+__global__ void __launch_bounds__(SCAN_THREADS) scan_tile_sums_kernel(const u32* __restrict__ in, int n,
+                                                                      u32* __restrict__ partial) {
+  __shared__ u32 ws[SCAN_WARPS];
+  const int base = blockIdx.x * SCAN_TILE, len = min(SCAN_TILE, n - base);
+  u32 s = 0;
+  for (int i = threadIdx.x; i < len; i += SCAN_THREADS) s += in[base + i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    u32 t = 0;
+    for (int w = 0; w < SCAN_WARPS; ++w) t += ws[w];
+    partial[blockIdx.x] = t;
+  }
+}
+
+// Tile t scanned from the exclusive prefix partial[t] of the tile sums.
+__global__ void __launch_bounds__(SCAN_THREADS) scan_tiles_kernel(const u32* in, u32* out, int n,
+                                                                  const u32* __restrict__ partial) {
+  __shared__ u32 ws[SCAN_WARPS];
+  const int base = blockIdx.x * SCAN_TILE;
+  tile_scan(in + base, out + base, min(SCAN_TILE, n - base), partial[blockIdx.x], ws);
+}
+
+// Radix histogram rows: CTA d scans row d (hist[d * nb + b] over the nb blocks) in place and
+// stores the row's total in rowtot[d].
+__global__ void __launch_bounds__(SCAN_THREADS) rs_rowscan_kernel(u32* hist, int nb, u32* __restrict__ rowtot) {
+  __shared__ u32 ws[SCAN_WARPS];
+  u32* row = hist + (size_t)blockIdx.x * nb;
+  u32 carry = 0;
+  for (int b = 0; b < nb; b += SCAN_TILE) carry += tile_scan(row + b, row + b, min(SCAN_TILE, nb - b), carry, ws);
+  if (threadIdx.x == 0) rowtot[blockIdx.x] = carry;
+}
+
+// hist: each digit row scanned by rs_rowscan_kernel, row totals in rowtot.  A block's first
+// slot for digit d = (sum of the row totals of digits below d) + hist[d * nblocks + block].
 __global__ void __launch_bounds__(RS_THREADS) rs_scatter_kernel(
     const u64* __restrict__ kin, const u32* __restrict__ vin, u64* __restrict__ kout,
     u32* __restrict__ vout, int n, int shift, u32 mask, const u32* __restrict__ hist,
-    int nblocks) {
+    const u32* __restrict__ rowtot, int nblocks) {
+  static_assert(RS_THREADS == 256, "one thread per digit");
   __shared__ u32 wh[RS_WARPS][256];
   __shared__ u32 gb[256];
+  __shared__ u32 wsum[RS_WARPS];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int i = threadIdx.x; i < RS_WARPS * 256; i += RS_THREADS) (&wh[0][0])[i] = 0;
-  for (int d = threadIdx.x; d <= (int)mask; d += RS_THREADS) gb[d] = hist[d * nblocks + blockIdx.x];
+  {
+    const int d = threadIdx.x;
+    const u32 t = d <= (int)mask ? rowtot[d] : 0u;
+    const u32 x = warp_incl_scan(t, lane);
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    u32 base = x - t;
+    for (int w = 0; w < warp; ++w) base += wsum[w];
+    if (d <= (int)mask) gb[d] = base + hist[(size_t)d * nblocks + blockIdx.x];
+  }
   __syncthreads();
   u64 k[RS_STRIPS];
   u32 v[RS_STRIPS], r[RS_STRIPS];
@@ -127,20 +212,23 @@ __global__ void __launch_bounds__(RS_THREADS) rs_scatter_kernel(
 }
 
 int radix_hist_blocks(int n) { return (n + RS_TILE - 1) / RS_TILE; }
+size_t radix_hist_words(int n) { return (size_t)256 * radix_hist_blocks(n) + 256; }
 
 // Sorts (keys, vals) by key bits [0, nbits).  Ping-pongs with the alternates; on return
-// *keys / *vals point at the sorted data (the pointers may have been swapped).
+// *keys / *vals point at the sorted data (the pointers may have been swapped).  hist holds
+// radix_hist_words(n) words: the 256 x blocks digit counts, then the 256 row totals.
 int radix_sort_pairs(u64** keys, u32** vals, u64** keys_alt, u32** vals_alt, u32* hist, int n,
                      int nbits, cudaStream_t st) {
   if (n <= 0) return PMGB_OK;
   const int nb = radix_hist_blocks(n);
+  u32* rowtot = hist + (size_t)256 * nb;
   for (int shift = 0; shift < nbits; shift += 8) {
     int bits = nbits - shift < 8 ? nbits - shift : 8;
     u32 mask = (1u << bits) - 1u;
     rs_hist_kernel<<<nb, RS_THREADS, 0, st>>>(*keys, n, shift, mask, hist, nb);
-    exclusive_scan_kernel<<<1, 1024, 0, st>>>(hist, hist, (int)(mask + 1) * nb, nullptr);
+    rs_rowscan_kernel<<<mask + 1, SCAN_THREADS, 0, st>>>(hist, nb, rowtot);
     rs_scatter_kernel<<<nb, RS_THREADS, 0, st>>>(*keys, *vals, *keys_alt, *vals_alt, n, shift,
-                                                 mask, hist, nb);
+                                                 mask, hist, rowtot, nb);
     PMGB_LAUNCH_CHECK();
     count_launches(3);
     u64* tk = *keys;
@@ -153,10 +241,25 @@ int radix_sort_pairs(u64** keys, u32** vals, u64** keys_alt, u32** vals_alt, u32
   return PMGB_OK;
 }
 
-int exclusive_scan(const u32* in, u32* out, int n, u32* total, cudaStream_t st) {
-  exclusive_scan_kernel<<<1, 1024, 0, st>>>(in, out, n, total);
+int scan_scratch_words(int n) { return n / SCAN_TILE + 2; }
+
+// out = exclusive scan of in[0, n) (in == out allowed), *total = the sum.  Up to 8 tiles one
+// CTA walks the array; beyond, tile sums, their scan and the tiles run as three launches with
+// the tile sums in scratch (scan_scratch_words(n) words).
+int exclusive_scan(const u32* in, u32* out, int n, u32* total, u32* scratch, cudaStream_t st) {
+  n = n < 0 ? 0 : n;
+  const int tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+  if (tiles <= 8) {
+    scan_serial_kernel<<<1, SCAN_THREADS, 0, st>>>(in, out, n, total);
+    PMGB_LAUNCH_CHECK();
+    count_launches(1);
+    return PMGB_OK;
+  }
+  scan_tile_sums_kernel<<<tiles, SCAN_THREADS, 0, st>>>(in, n, scratch);
+  scan_serial_kernel<<<1, SCAN_THREADS, 0, st>>>(scratch, scratch, tiles, total);
+  scan_tiles_kernel<<<tiles, SCAN_THREADS, 0, st>>>(in, out, n, scratch);
   PMGB_LAUNCH_CHECK();
-  count_launches(1);
+  count_launches(3);
   return PMGB_OK;
 }
 
