@@ -61,7 +61,10 @@ __global__ void __launch_bounds__(DEP_THREADS) ens_deposit_kernel(const EnsSys* 
   }
 }
 
-__global__ void __launch_bounds__(FFT_THREADS) ens_fft_x_r2c_kernel(const EnsSys* __restrict__ sys,
+// The FFT passes of all systems' meshes share one kernel each (a switch on the transform length
+// inside): capped at 80 registers, 3 CTAs per SM, so the largest length's code sets no lower
+// occupancy for the rest.
+__global__ void __launch_bounds__(FFT_THREADS, 3) ens_fft_x_r2c_kernel(const EnsSys* __restrict__ sys,
                                                                     const int2* __restrict__ items,
                                                                     int nitems, u64* __restrict__ rho,
                                                                     float2* __restrict__ spec,
@@ -77,7 +80,7 @@ __global__ void __launch_bounds__(FFT_THREADS) ens_fft_x_r2c_kernel(const EnsSys
   }
 }
 
-__global__ void __launch_bounds__(FFT_THREADS) ens_fft_x_c2r_kernel(const EnsSys* __restrict__ sys,
+__global__ void __launch_bounds__(FFT_THREADS, 3) ens_fft_x_c2r_kernel(const EnsSys* __restrict__ sys,
                                                                     const int2* __restrict__ items,
                                                                     int nitems,
                                                                     const float2* __restrict__ spec,
@@ -95,7 +98,7 @@ __global__ void __launch_bounds__(FFT_THREADS) ens_fft_x_c2r_kernel(const EnsSys
 }
 
 // items: (system, kx0, other) for one axis
-__global__ void __launch_bounds__(FFT_THREADS) ens_fft_cols_kernel(const EnsSys* __restrict__ sys,
+__global__ void __launch_bounds__(FFT_THREADS, 3) ens_fft_cols_kernel(const EnsSys* __restrict__ sys,
                                                                    const int4* __restrict__ items,
                                                                    int nitems, float2* __restrict__ spec,
                                                                    int axis, int mode,

@@ -24,6 +24,7 @@
 
 namespace pmgb {
 
+template <int LOGN>
 __global__ void __launch_bounds__(FFT_THREADS) fft_x_r2c_kernel(u64* __restrict__ rho,
                                                                 float2* __restrict__ spec,
                                                                 MeshDims m, int pairs,
@@ -34,9 +35,10 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_x_r2c_kernel(u64* __restrict_
                                                                 float* __restrict__ rho_copy) {
   if (stop && *stop) return;
   extern __shared__ float2 sm[];
-  fft_x_r2c_body(sm, rho, spec, m, pairs, fx_inv, twg, nmax, 2ll * blockIdx.x * pairs, rho_copy);
+  x_r2c_t<LOGN>(sm, rho, spec, m, pairs, fx_inv, twg, nmax, 2ll * blockIdx.x * pairs, rho_copy);
 }
 
+template <int LOGN>
 __global__ void __launch_bounds__(FFT_THREADS) fft_x_c2r_kernel(const float2* __restrict__ spec,
                                                                 float* __restrict__ phi,
                                                                 MeshDims m, int pairs,
@@ -45,9 +47,10 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_x_c2r_kernel(const float2* __
                                                                 const int* __restrict__ stop) {
   if (stop && *stop) return;
   extern __shared__ float2 sm[];
-  fft_x_c2r_body(sm, spec, phi, m, pairs, twg, nmax, 2ll * blockIdx.x * pairs);
+  x_c2r_t<LOGN>(sm, spec, phi, m, pairs, twg, nmax, 2ll * blockIdx.x * pairs);
 }
 
+template <int LOGN>
 __global__ void __launch_bounds__(FFT_THREADS) fft_cols_kernel(float2* __restrict__ spec,
                                                                MeshDims m, int axis, int mode,
                                                                const float* __restrict__ ghat,
@@ -56,26 +59,36 @@ __global__ void __launch_bounds__(FFT_THREADS) fft_cols_kernel(float2* __restric
                                                                const int* __restrict__ stop) {
   if (stop && *stop) return;
   extern __shared__ float2 sm[];
-  fft_cols_body(sm, spec, m, axis, mode, ghat, twg, nmax, blockIdx.x * COL_TX, blockIdx.y);
+  cols_t<LOGN>(sm, spec, m, axis, mode, ghat, twg, nmax, blockIdx.x * COL_TX, blockIdx.y);
 }
+
+// The kernels of one transform length, picked on the host.
+struct FftKernels {
+  void (*r2c)(u64*, float2*, MeshDims, int, float, const float2*, int, const int*, float*);
+  void (*c2r)(const float2*, float*, MeshDims, int, const float2*, int, const int*);
+  void (*cols)(float2*, MeshDims, int, int, const float*, const float2*, int, const int*);
+};
+template <int LOGN>
+constexpr FftKernels fft_kernels_t() {
+  return {fft_x_r2c_kernel<LOGN>, fft_x_c2r_kernel<LOGN>, fft_cols_kernel<LOGN>};
+}
+static const FftKernels kFft[10] = {{}, {}, {}, fft_kernels_t<3>(), fft_kernels_t<4>(), fft_kernels_t<5>(),
+                                    fft_kernels_t<6>(), fft_kernels_t<7>(), fft_kernels_t<8>(), fft_kernels_t<9>()};
 
 // ---------------------------------------------------------------- host side ----------
 static int x_pairs(const MeshDims& m) { return x_pairs_default(m); }
 
-int fft_smem_bytes_max(const MeshDims& m) {
-  int a = x_smem_elems(m.nx, x_pairs(m)) * (int)sizeof(float2);
-  int ny = col_smem_elems(m.ny) * (int)sizeof(float2);
-  int nz = col_smem_elems(m.nz) * (int)sizeof(float2);
-  return a > ny ? (a > nz ? a : nz) : (ny > nz ? ny : nz);
-}
-
 int fft_configure(const MeshDims& m) {
-  int bytes = fft_smem_bytes_max(m);
-  if (bytes > 48 * 1024) {
-    PMGB_CUDA_TRY(cudaFuncSetAttribute(fft_x_r2c_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-    PMGB_CUDA_TRY(cudaFuncSetAttribute(fft_x_c2r_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-    PMGB_CUDA_TRY(cudaFuncSetAttribute(fft_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  const int xs = x_smem_elems(m.nx, x_pairs(m)) * (int)sizeof(float2);
+  const int ys = col_smem_elems(m.ny) * (int)sizeof(float2), zs = col_smem_elems(m.nz) * (int)sizeof(float2);
+  if (xs > 48 * 1024) {
+    PMGB_CUDA_TRY(cudaFuncSetAttribute(kFft[m.lx].r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, xs));
+    PMGB_CUDA_TRY(cudaFuncSetAttribute(kFft[m.lx].c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, xs));
   }
+  if (ys > 48 * 1024)
+    PMGB_CUDA_TRY(cudaFuncSetAttribute(kFft[m.ly].cols, cudaFuncAttributeMaxDynamicSharedMemorySize, ys));
+  if (zs > 48 * 1024)
+    PMGB_CUDA_TRY(cudaFuncSetAttribute(kFft[m.lz].cols, cudaFuncAttributeMaxDynamicSharedMemorySize, zs));
   return PMGB_OK;
 }
 
@@ -89,11 +102,14 @@ int launch_poisson(u64* rho, float2* spec, float* phi, const float* ghat, const 
   const int ctiles = (m.nxp + COL_TX - 1) / COL_TX;
   const int ysmem = col_smem_elems(m.ny) * (int)sizeof(float2);
   const int zsmem = col_smem_elems(m.nz) * (int)sizeof(float2);
-  fft_x_r2c_kernel<<<xblocks, FFT_THREADS, xsmem, st>>>(rho, spec, m, pairs, fx_inv, tw, nmax, stop, rho_copy);
-  fft_cols_kernel<<<dim3(ctiles, m.nz), FFT_THREADS, ysmem, st>>>(spec, m, 1, 0, nullptr, tw, nmax, stop);
-  fft_cols_kernel<<<dim3(ctiles, m.ny), FFT_THREADS, zsmem, st>>>(spec, m, 2, 2, ghat, tw, nmax, stop);
-  fft_cols_kernel<<<dim3(ctiles, m.nz), FFT_THREADS, ysmem, st>>>(spec, m, 1, 1, nullptr, tw, nmax, stop);
-  fft_x_c2r_kernel<<<xblocks, FFT_THREADS, xsmem, st>>>(spec, phi, m, pairs, tw, nmax, stop);
+  const FftKernels& kx = kFft[m.lx];
+  const FftKernels& ky = kFft[m.ly];
+  const FftKernels& kz = kFft[m.lz];
+  kx.r2c<<<xblocks, FFT_THREADS, xsmem, st>>>(rho, spec, m, pairs, fx_inv, tw, nmax, stop, rho_copy);
+  ky.cols<<<dim3(ctiles, m.nz), FFT_THREADS, ysmem, st>>>(spec, m, 1, 0, nullptr, tw, nmax, stop);
+  kz.cols<<<dim3(ctiles, m.ny), FFT_THREADS, zsmem, st>>>(spec, m, 2, 2, ghat, tw, nmax, stop);
+  ky.cols<<<dim3(ctiles, m.nz), FFT_THREADS, ysmem, st>>>(spec, m, 1, 1, nullptr, tw, nmax, stop);
+  kx.c2r<<<xblocks, FFT_THREADS, xsmem, st>>>(spec, phi, m, pairs, tw, nmax, stop);
   PMGB_LAUNCH_CHECK();
   count_launches(5);
   return PMGB_OK;
