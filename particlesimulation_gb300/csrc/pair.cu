@@ -245,15 +245,17 @@ struct SlotI {
   float px, py, pz;
 };
 
+// tab_base: shared-memory address of this lane's table copy minus bits(kMagic) * SLOT_REP * 8,
+// so that segment t = bits(kMagic + t) - bits(kMagic) is at bits(kMagic + t) * SLOT_REP * 8 +
+// tab_base (32-bit arithmetic modulo 2^32): one multiply-add per lookup.
 template <bool EQM>
-__device__ __forceinline__ void slot_pair(SlotI& I, const float4& q, float inv_d2,
-                                          const float2* __restrict__ tab) {
+__device__ __forceinline__ void slot_pair(SlotI& I, const float4& q, float inv_d2, u32 tab_base) {
   const float dx = I.p.x - q.x, dy = I.p.y - q.y, dz = I.p.z - q.z;
   const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
   const float xi = fminf(r2 * inv_d2, 499.5f);
-  const float tf = __fadd_rd(xi, kMagic);  // kMagic + floor(xi)
-  const int t = __float_as_int(tf) - __float_as_int(kMagic);
-  const float2 ab = tab[t * SLOT_REP];  // tab already points at this lane's copy
+  const u32 bits = __float_as_uint(__fadd_rd(xi, kMagic));  // kMagic + floor(xi)
+  float2 ab;
+  asm("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(ab.x), "=f"(ab.y) : "r"(bits * (SLOT_REP * 8) + tab_base));
   float f = fmaf(xi, ab.y, ab.x);
   if (!EQM) f *= q.w;
   I.px = fmaf(f, dx, I.px);
@@ -317,7 +319,8 @@ __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
-  const float2* tab = tab_all + (lane & (SLOT_REP - 1));
+  const u32 tab_base = (u32)__cvta_generic_to_shared(tab_all + (lane & (SLOT_REP - 1))) -
+                       __float_as_uint(kMagic) * (u32)(SLOT_REP * 8);
   const u32 nitems = *nitems_p * NNB;  // every slice once per neighbour cell
   const float inv_d2 = pp.inv_d2;
   const int sub = cd.sub, sub2 = sub * sub;
@@ -380,7 +383,7 @@ __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
           for (int s = 0; s < cnt; ++s) {
             const float4 q = jbuf[warp][s];
 #pragma unroll
-            for (int u = 0; u < SLOT_IPL; ++u) slot_pair<EQM>(I[u], q, inv_d2, tab);
+            for (int u = 0; u < SLOT_IPL; ++u) slot_pair<EQM>(I[u], q, inv_d2, tab_base);
           }
           __syncwarp();
 #pragma unroll
