@@ -220,7 +220,11 @@ __global__ void __launch_bounds__(PAIR_THREADS) pair_kernel(
 //  * the table is kept in intercept form per segment, f(xi) = A[t] + xi S[t] with
 //    S[t] = T[t+1] - T[t] (float, as the reference forms it) and A[t] = T[t] - t S[t] (double,
 //    rounded once): one FMA instead of forming xi - t;
-//  * t = floor(xi) is one round-down add of 1.5 * 2^23 (FADD.RM) and an integer subtract;
+//  * positions enter in units of the table spacing delta, relative to the slice's first
+//    particle (so differences keep code-unit precision): |r|^2 is xi, and 1/delta is folded into
+//    the table;
+//  * t = floor(xi) is one round-down add of 1.5 * 2^23 (FADD.RM), whose bits give the lane's
+//    table entry by one 32-bit multiply-add into a shared-memory address;
 //  * the cutoff test is folded into the table: segments t >= 499 (xi >= 499, i.e.
 //    r^2 >= re^2) are zero, and xi is clamped to 499.5 so t never leaves the table;
 //  * with equal masses (every benchmark workload) the mass is folded into the table;
@@ -248,11 +252,12 @@ struct SlotI {
 // tab_base: shared-memory address of this lane's table copy minus bits(kMagic) * SLOT_REP * 8,
 // so that segment t = bits(kMagic + t) - bits(kMagic) is at bits(kMagic + t) * SLOT_REP * 8 +
 // tab_base (32-bit arithmetic modulo 2^32): one multiply-add per lookup.
+// Positions are in units of the table spacing delta (relative to the slice's first particle), so
+// |r|^2 is xi itself; the table holds f / delta for the unscaled difference vector.
 template <bool EQM>
-__device__ __forceinline__ void slot_pair(SlotI& I, const float4& q, float inv_d2, u32 tab_base) {
+__device__ __forceinline__ void slot_pair(SlotI& I, const float4& q, u32 tab_base) {
   const float dx = I.p.x - q.x, dy = I.p.y - q.y, dz = I.p.z - q.z;
-  const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-  const float xi = fminf(r2 * inv_d2, 499.5f);
+  const float xi = fminf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)), 499.5f);
   const u32 bits = __float_as_uint(__fadd_rd(xi, kMagic));  // kMagic + floor(xi)
   float2 ab;
   asm("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(ab.x), "=f"(ab.y) : "r"(bits * (SLOT_REP * 8) + tab_base));
@@ -301,9 +306,11 @@ __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
   extern __shared__ float4 slot_smem[];
   float4 (*jbuf)[32] = reinterpret_cast<float4 (*)[32]>(slot_smem);
   float2* tab_all = reinterpret_cast<float2*>(slot_smem + SLOT_WARPS * 32);
+  // coordinates are scaled by sc = 1/delta (sc^2 = 1/delta^2 to float rounding)
+  const float sc = (float)sqrt((double)pp.inv_d2);
   {
-    // every particle has the same mass when EQM: fold it into the table
-    const double mj = EQM ? (double)__ldg(&pm[0].w) : 1.0;
+    // every particle has the same mass when EQM: fold it into the table, with 1/sc
+    const double mj = (EQM ? (double)__ldg(&pm[0].w) : 1.0) / (double)sc;
     for (int t = threadIdx.x; t < SLOT_TAB; t += SLOT_THREADS) {
       float2 ab = make_float2(0.f, 0.f);
       if (t < 499) {
@@ -322,7 +329,6 @@ __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
   const u32 tab_base = (u32)__cvta_generic_to_shared(tab_all + (lane & (SLOT_REP - 1))) -
                        __float_as_uint(kMagic) * (u32)(SLOT_REP * 8);
   const u32 nitems = *nitems_p * NNB;  // every slice once per neighbour cell
-  const float inv_d2 = pp.inv_d2;
   const int sub = cd.sub, sub2 = sub * sub;
   // a neighbour sub-column is skipped when its x-z distance from the slice's sub-column is at
   // least the cutoff (with a margin far above the rounding of the sub-column assignment)
@@ -353,6 +359,15 @@ __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
       // y range of the slice: its first particle (lane 0, u = 0) and its last one
       const float ys0 = __shfl_sync(0xFFFFFFFFu, I[0].p.y, 0);
       const float ys1 = __ldg(&pm[last].y);
+      // origin of the scaled coordinates: the slice's first particle (near every pair's ends, so
+      // the differences keep the precision of code-unit differences)
+      const float ox = __shfl_sync(0xFFFFFFFFu, I[0].p.x, 0), oz = __shfl_sync(0xFFFFFFFFu, I[0].p.z, 0);
+#pragma unroll
+      for (int u = 0; u < SLOT_IPL; ++u) {
+        I[u].p.x = (I[u].p.x - ox) * sc;
+        I[u].p.y = (I[u].p.y - ys0) * sc;
+        I[u].p.z = (I[u].p.z - oz) * sc;
+      }
       if (nx >= 0 && ny >= 0 && nz >= 0 && nx < cd.Mx && ny < cd.My && nz < cd.Mz)
       for (int qs = 0; qs < sub2; ++qs) {
         const int jsx = qs % sub, jsz = qs / sub;
@@ -374,7 +389,11 @@ __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
         }
         for (int j0 = b; j0 < e; j0 += 32) {
           const int jj = j0 + lane;
-          jbuf[warp][lane] = jj < e ? pm[jj] : make_float4(3.0e30f, 3.0e30f, 3.0e30f, 0.f);
+          float4 qj = jj < e ? pm[jj] : make_float4(3.0e30f, 3.0e30f, 3.0e30f, 0.f);
+          qj.x = (qj.x - ox) * sc;
+          qj.y = (qj.y - ys0) * sc;
+          qj.z = (qj.z - oz) * sc;
+          jbuf[warp][lane] = qj;
           __syncwarp();
           const int cnt = min(32, e - j0);
 #pragma unroll
@@ -383,7 +402,7 @@ __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
           for (int s = 0; s < cnt; ++s) {
             const float4 q = jbuf[warp][s];
 #pragma unroll
-            for (int u = 0; u < SLOT_IPL; ++u) slot_pair<EQM>(I[u], q, inv_d2, tab_base);
+            for (int u = 0; u < SLOT_IPL; ++u) slot_pair<EQM>(I[u], q, tab_base);
           }
           __syncwarp();
 #pragma unroll
