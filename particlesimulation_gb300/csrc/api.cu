@@ -184,7 +184,8 @@ int force(pmgb_pm* h, int kdk, float kick, int drift, int tag, bool timed) {
   }
   // ev[4] is recorded just before the pair kernel (after its work-item setup)
   rc = launch_pair(h->pm[h->cur], h->vi[h->cur], h->acc_pm, q->cell_start, q->cd,
-                   q->item_cnt, q->item_off, q->scan_tmp, q->nitems, q->items, q->counter, q->pp, q->table, sp,
+                   q->item_cnt, q->item_off, q->scan_tmp, q->nitems, q->items, q->nitems_max, q->heavy,
+                   q->counter, q->pp, q->table, sp,
                    kick, drift, kdk, h->pm[1 - h->cur], h->vi[1 - h->cur], h->acc,
                    q->count_pairs ? q->npairs : nullptr, stop,
                    h->num_sms, timed ? h->ev[4] : nullptr, h->st, h->equal_mass, q->slots, n);
@@ -630,13 +631,15 @@ int p3m_create_internal(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out,
   q->pp.eps2 = eps * eps;
   const size_t ntot = (size_t)q->nsub + 1;  // sub-columns + the bucket outside the mesh
   int rc;
+  // slices of sub-columns (32 particles for pair counting / the direct formula, 64 for the
+  // table pass, which takes each slice once per neighbour cell), the table pass's list of heavy
+  // units, and its 27 partial-force slots per particle
+  q->nitems_max = (int)((size_t)pm->n / 32 + ntot + 32);
   if ((rc = dalloc(&q->cell_start, ntot + 1)) || (rc = dalloc(&q->item_cnt, ntot)) ||
-      (rc = dalloc(&q->item_off, ntot)) || (rc = dalloc(&q->nitems, 1)) || (rc = dalloc(&q->counter, 1)) ||
+      (rc = dalloc(&q->item_off, ntot)) || (rc = dalloc(&q->nitems, 1)) || (rc = dalloc(&q->counter, 3)) ||
       (rc = dalloc(&q->scan_tmp, (size_t)scan_scratch_words((int)ntot))) ||
-      // slices of sub-columns (32 particles for pair counting / the direct formula, 64 for the
-      // table pass, which takes each slice once per neighbour cell), and the table pass's 27
-      // partial-force slots per particle
-      (rc = dalloc(&q->items, (size_t)pm->n / 32 + ntot + 32)) ||
+      (rc = dalloc(&q->items, (size_t)q->nitems_max)) ||
+      (rc = dalloc(&q->heavy, (size_t)slot_heavy_capacity(q->nitems_max))) ||
       (rc = dalloc(&q->table, 500)) || (rc = dalloc(&q->npairs, 1)) ||
       (rc = dalloc(&q->slots, 27 * (size_t)std::max(pm->n, 1)))) {
     pmgb_p3m_destroy(q);
@@ -664,7 +667,7 @@ int pmgb_p3m_destroy(pmgb_p3m* q) {
     q->pm->since_sort = 1 << 30;
   }
   void* ptrs[] = {q->cell_start, q->item_cnt, q->item_off, q->scan_tmp, q->nitems, q->counter, q->items, q->table,
-                  q->npairs, q->slots};
+                  q->npairs, q->slots, q->heavy};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete q;

@@ -10,6 +10,7 @@ size_t radix_hist_words(int n);  // size of radix_sort_pairs' hist buffer
 int radix_sort_pairs(u64** keys, u32** vals, u64** keys_alt, u32** vals_alt, u32* hist, int n,
                      int nbits, cudaStream_t st);
 int scan_scratch_words(int n);   // size of exclusive_scan's scratch buffer
+int slot_heavy_capacity(int nitems_max);  // entries of the pair pass's heavy-unit list
 int exclusive_scan(const u32* in, u32* out, int n, u32* total, u32* scratch, cudaStream_t st);
 int launch_chain_keys(const float4* pm, const float4* vi, int n, ChainDims c, int ysort,
                       const int* stop, u64* keys, u32* vals, cudaStream_t st);
@@ -37,9 +38,9 @@ int launch_pack(const float* pos, const float* vel, const float* mass_code, int 
                 float DT, int orig, float4* pm, float4* vi, cudaStream_t st);
 int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const int* cell_start,
                 const ChainDims& cd, u32* item_cnt, u32* item_off, u32* scan_tmp, u32* nitems, int2* items,
-                u32* counter, const PairParams& pp, const float* table, const StepParams& sp,
-                float kick, int drift, int kdk, float4* pm_out, float4* vi_out, float4* acc_out,
-                unsigned long long* npairs, int* stop, int num_sms, cudaEvent_t ev_pair,
+                int nitems_max, u32* heavy, u32* counter, const PairParams& pp, const float* table,
+                const StepParams& sp, float kick, int drift, int kdk, float4* pm_out, float4* vi_out,
+                float4* acc_out, unsigned long long* npairs, int* stop, int num_sms, cudaEvent_t ev_pair,
                 cudaStream_t st, int equal_mass, float4* slots, int n);
 
 }  // namespace pmgb
@@ -93,6 +94,8 @@ struct pmgb_p3m {
   pmgb::u32 *item_cnt = nullptr, *item_off = nullptr, *nitems = nullptr, *counter = nullptr;
   pmgb::u32* scan_tmp = nullptr;  // scratch of the item-count scan (scan_scratch_words)
   int2* items = nullptr;
+  int nitems_max = 0;             // capacity of items
+  pmgb::u32* heavy = nullptr;     // heavy units of the table pass (slot_heavy_capacity entries)
   float* table = nullptr;
   float table_h[500];
   float delta2 = 0;

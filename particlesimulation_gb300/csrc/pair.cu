@@ -241,7 +241,10 @@ constexpr int SLOT_REP = 16;                 // table copies (lane mod 16)
 constexpr int NNB = 27;                      // neighbour cells (and slots) per particle
 constexpr int SLOT_THREADS = 512;
 constexpr int SLOT_WARPS = SLOT_THREADS / 32;
-constexpr int SLOT_SMEM = SLOT_TAB * SLOT_REP * 8 + SLOT_WARPS * 32 * 16;  // table + staging
+// staging (SLOT_WARPS x 32 float4) + CTA partial sums (SLOT_WARPS x SLOT_SLICE float4) + table
+constexpr int SLOT_SMEM = SLOT_WARPS * 32 * 16 + SLOT_WARPS * SLOT_SLICE * 16 + SLOT_TAB * SLOT_REP * 8;
+// Cells with at least this many particles: their slices' units are taken by whole CTAs.
+constexpr int SLOT_HEAVY_POP = 16384;
 
 struct SlotI {
   float4 p;
@@ -296,16 +299,169 @@ __device__ __forceinline__ int warp_y_bound(const float4* __restrict__ pm, int l
   return lo + __popc(__ballot_sync(0xFFFFFFFFu, below));
 }
 
+// A unit is heavy when its neighbour cell holds at least SLOT_HEAVY_POP particles: its slice
+// then meets up to that many candidates per particle (a whole warp's share of the pass on the
+// bulge of the disk workloads), so whole CTAs take the heavy units first.
+__device__ __forceinline__ bool slot_heavy(const int* __restrict__ cell_start, const ChainDimsP& cd,
+                                           int2 item, int k) {
+  const int sub2 = cd.sub * cd.sub;
+  const int cell = item.x / sub2;
+  if (cell >= cd.ncells) return false;
+  const int gx = cell % cd.Mx, gy = (cell / cd.Mx) % cd.My, gz = cell / (cd.Mx * cd.My);
+  const int nx = gx + k % 3 - 1, ny = gy + (k / 3) % 3 - 1, nz = gz + k / 9 - 1;
+  if (nx < 0 || ny < 0 || nz < 0 || nx >= cd.Mx || ny >= cd.My || nz >= cd.Mz) return false;
+  const int nb = nx + ny * cd.Mx + nz * cd.Mx * cd.My;
+  return __ldg(&cell_start[(nb + 1) * sub2]) - __ldg(&cell_start[nb * sub2]) >= SLOT_HEAVY_POP;
+}
+
+// Per-launch constants of the table pass.
+struct SlotCtx {
+  const float4* __restrict__ pm;
+  const int* __restrict__ cell_start;
+  const int2* __restrict__ items;
+  float4* __restrict__ slots;
+  int n;
+  ChainDimsP cd;
+  float re2, sc, gap_margin;
+  int ysort;
+};
+
+// One work unit: the slice items[it / 27] against neighbour cell it % 27, into slot k of the
+// slice's particles.  COOP: every warp of the CTA takes the unit, warp w the candidate chunks
+// c = w, w + SLOT_WARPS, ... (chunks of 32 counted across the neighbour's sub-columns), and the
+// warps' partial sums are added in warp order through shared memory (part: SLOT_WARPS x
+// SLOT_SLICE), so the result does not depend on timing.
+template <bool EQM, bool COOP>
+__device__ __forceinline__ void slot_unit(const SlotCtx& c, u32 it, float4 (*jbuf)[32], float4* part,
+                                          u32 tab_base, int lane, int warp) {
+  const ChainDimsP& cd = c.cd;
+  const int sub = cd.sub, sub2 = sub * sub;
+  const int2 item = c.items[it / NNB];
+  const int k = (int)(it % NNB);
+  const int cell = item.x / sub2;
+  const int cend = c.cell_start[item.x + 1];
+  const int last = min(item.y + SLOT_SLICE - 1, cend - 1);
+  SlotI I[SLOT_IPL];
+#pragma unroll
+  for (int u = 0; u < SLOT_IPL; ++u) {
+    const int i = item.y + 32 * u + lane;
+    I[u].p = c.pm[i < cend ? i : last];
+    I[u].sx = I[u].sy = I[u].sz = I[u].cx = I[u].cy = I[u].cz = 0.f;
+  }
+  if (cell < cd.ncells) {
+    const int gx = cell % cd.Mx, gy = (cell / cd.Mx) % cd.My, gz = cell / (cd.Mx * cd.My);
+    const int nx = gx + k % 3 - 1, ny = gy + (k / 3) % 3 - 1, nz = gz + k / 9 - 1;
+    // the slice's sub-column: x and z ranges in code units
+    const int isx = item.x % sub, isz = (item.x / sub) % sub;
+    const float ix0 = (gx * sub + isx) * cd.HCsx, iz0 = (gz * sub + isz) * cd.HCsz;
+    // y range of the slice: its first particle (lane 0, u = 0) and its last one
+    const float ys0 = __shfl_sync(0xFFFFFFFFu, I[0].p.y, 0);
+    const float ys1 = __ldg(&c.pm[last].y);
+    // origin of the scaled coordinates: the slice's first particle (near every pair's ends, so
+    // the differences keep the precision of code-unit differences)
+    const float ox = __shfl_sync(0xFFFFFFFFu, I[0].p.x, 0), oz = __shfl_sync(0xFFFFFFFFu, I[0].p.z, 0);
+    const float sc = c.sc;
+#pragma unroll
+    for (int u = 0; u < SLOT_IPL; ++u) {
+      I[u].p.x = (I[u].p.x - ox) * sc;
+      I[u].p.y = (I[u].p.y - ys0) * sc;
+      I[u].p.z = (I[u].p.z - oz) * sc;
+    }
+    int chunk = 0;  // COOP: candidate chunks met so far in this unit
+    if (nx >= 0 && ny >= 0 && nz >= 0 && nx < cd.Mx && ny < cd.My && nz < cd.Mz)
+    for (int qs = 0; qs < sub2; ++qs) {
+      const int jsx = qs % sub, jsz = qs / sub;
+      const float jx0 = (nx * sub + jsx) * cd.HCsx, jz0 = (nz * sub + jsz) * cd.HCsz;
+      const float gxs = fmaxf(fmaxf(jx0 - (ix0 + cd.HCsx), ix0 - (jx0 + cd.HCsx)) - c.gap_margin, 0.f);
+      const float gzs = fmaxf(fmaxf(jz0 - (iz0 + cd.HCsz), iz0 - (jz0 + cd.HCsz)) - c.gap_margin, 0.f);
+      const float g2 = gxs * gxs + gzs * gzs;
+      if (g2 >= c.re2) continue;
+      // a pair in range has |dy|^2 < re^2 - (its x-z distance)^2 <= re^2 - g2: the y window
+      // of this sub-column is the chord of the cutoff sphere at the sub-column's x-z gap, widened
+      // by 1e-5 of the coordinates' size against float rounding of the comparisons
+      const float h = sqrtf(c.re2 - g2) + 1e-5f * (1.f + fabsf(ys1));
+      const int cn = (nx + ny * cd.Mx + nz * cd.Mx * cd.My) * sub2 + qs;
+      int b = c.cell_start[cn];
+      int e = c.cell_start[cn + 1];
+      if (c.ysort && e > b) {
+        b = warp_y_bound<false>(c.pm, b, e, ys0 - h, lane);
+        e = warp_y_bound<true>(c.pm, b, e, ys1 + h, lane);
+      }
+      for (int j0 = b; j0 < e; j0 += 32) {
+        if (COOP) {
+          const bool mine = (chunk & (SLOT_WARPS - 1)) == warp;
+          ++chunk;
+          if (!mine) continue;
+        }
+        const int jj = j0 + lane;
+        float4 qj = jj < e ? c.pm[jj] : make_float4(3.0e30f, 3.0e30f, 3.0e30f, 0.f);
+        qj.x = (qj.x - ox) * sc;
+        qj.y = (qj.y - ys0) * sc;
+        qj.z = (qj.z - oz) * sc;
+        jbuf[warp][lane] = qj;
+        __syncwarp();
+        const int cnt = min(32, e - j0);
+#pragma unroll
+        for (int u = 0; u < SLOT_IPL; ++u) I[u].px = I[u].py = I[u].pz = 0.f;
+#pragma unroll 4
+        for (int s = 0; s < cnt; ++s) {
+          const float4 q = jbuf[warp][s];
+#pragma unroll
+          for (int u = 0; u < SLOT_IPL; ++u) slot_pair<EQM>(I[u], q, tab_base);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int u = 0; u < SLOT_IPL; ++u) {
+          kahan_add(I[u].sx, I[u].cx, I[u].px);
+          kahan_add(I[u].sy, I[u].cy, I[u].py);
+          kahan_add(I[u].sz, I[u].cz, I[u].pz);
+        }
+      }
+    }
+  }
+  if (!COOP) {
+#pragma unroll
+    for (int u = 0; u < SLOT_IPL; ++u) {
+      const int i = item.y + 32 * u + lane;
+      if (i < cend) c.slots[(size_t)k * c.n + i] = make_float4(I[u].sx, I[u].sy, I[u].sz, 0.f);
+    }
+  } else {
+#pragma unroll
+    for (int u = 0; u < SLOT_IPL; ++u)
+      part[warp * SLOT_SLICE + 32 * u + lane] = make_float4(I[u].sx, I[u].sy, I[u].sz, 0.f);
+    __syncthreads();
+    if (threadIdx.x < SLOT_SLICE) {
+      float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+#pragma unroll 4
+      for (int w = 0; w < SLOT_WARPS; ++w) {
+        const float4 v = part[w * SLOT_SLICE + threadIdx.x];
+        kahan_add(sx, cx, v.x);
+        kahan_add(sy, cy, v.y);
+        kahan_add(sz, cz, v.z);
+      }
+      const int i = item.y + (int)threadIdx.x;
+      if (i < cend) c.slots[(size_t)k * c.n + i] = make_float4(sx, sy, sz, 0.f);
+    }
+    __syncthreads();
+  }
+}
+
+// The heavy units listed by plan_heavy_kernel (heavy[0, counter[2])) are taken first, each by a
+// whole CTA (counter[0]), so that no single warp is left with a unit of tens of thousands of
+// candidates per particle while the others idle; then every warp takes the other units one at a
+// time (counter[1]).  If the list overflowed its capacity, no unit is treated as heavy.
 template <bool EQM>
 __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
     const float4* __restrict__ pm, int n, const int* __restrict__ cell_start,
-    const int2* __restrict__ items, const u32* __restrict__ nitems_p, u32* __restrict__ counter,
-    ChainDimsP cd, PairParams pp, const float* __restrict__ table, float4* __restrict__ slots,
-    const int* __restrict__ stop) {
+    const int2* __restrict__ items, const u32* __restrict__ nitems_p, const u32* __restrict__ heavy,
+    u32 heavy_cap, u32* __restrict__ counter, ChainDimsP cd, PairParams pp, const float* __restrict__ table,
+    float4* __restrict__ slots, const int* __restrict__ stop) {
   if (*stop) return;
   extern __shared__ float4 slot_smem[];
+  __shared__ u32 s_unit;
   float4 (*jbuf)[32] = reinterpret_cast<float4 (*)[32]>(slot_smem);
-  float2* tab_all = reinterpret_cast<float2*>(slot_smem + SLOT_WARPS * 32);
+  float4* part = slot_smem + SLOT_WARPS * 32;
+  float2* tab_all = reinterpret_cast<float2*>(part + SLOT_WARPS * SLOT_SLICE);
   // coordinates are scaled by sc = 1/delta (sc^2 = 1/delta^2 to float rounding)
   const float sc = (float)sqrt((double)pp.inv_d2);
   {
@@ -328,97 +484,28 @@ __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
   const int warp = threadIdx.x >> 5;
   const u32 tab_base = (u32)__cvta_generic_to_shared(tab_all + (lane & (SLOT_REP - 1))) -
                        __float_as_uint(kMagic) * (u32)(SLOT_REP * 8);
-  const u32 nitems = *nitems_p * NNB;  // every slice once per neighbour cell
-  const int sub = cd.sub, sub2 = sub * sub;
   // a neighbour sub-column is skipped when its x-z distance from the slice's sub-column is at
   // least the cutoff (with a margin far above the rounding of the sub-column assignment)
-  const float gap_margin = 1e-3f * fminf(cd.HCsx, cd.HCsz);
+  const SlotCtx c{pm, cell_start, items, slots, n, cd, pp.re2, sc, 1e-3f * fminf(cd.HCsx, cd.HCsz), pp.ysort};
+  const u32 nall = *nitems_p * NNB;  // every slice once per neighbour cell
+  const u32 nlisted = __ldcg(&counter[2]);
+  const bool listed = nlisted <= heavy_cap;  // the heavy units are all in the list
+  const u32 nheavy = listed ? nlisted : 0u;
+  for (;;) {
+    if (threadIdx.x == 0) s_unit = atomicAdd(&counter[0], 1u);
+    __syncthreads();
+    const u32 h = s_unit;
+    __syncthreads();
+    if (h >= nheavy) break;
+    slot_unit<EQM, true>(c, __ldg(&heavy[h]), jbuf, part, tab_base, lane, warp);
+  }
   for (;;) {
     u32 it = 0;
-    if (lane == 0) it = atomicAdd(counter, 1u);
+    if (lane == 0) it = atomicAdd(&counter[1], 1u);
     it = __shfl_sync(0xFFFFFFFFu, it, 0);
-    if (it >= nitems) break;
-    const int2 item = items[it / NNB];
-    const int k = (int)(it % NNB);
-    const int cell = item.x / sub2;
-    const int cend = cell_start[item.x + 1];
-    const int last = min(item.y + SLOT_SLICE - 1, cend - 1);
-    SlotI I[SLOT_IPL];
-#pragma unroll
-    for (int u = 0; u < SLOT_IPL; ++u) {
-      const int i = item.y + 32 * u + lane;
-      I[u].p = pm[i < cend ? i : last];
-      I[u].sx = I[u].sy = I[u].sz = I[u].cx = I[u].cy = I[u].cz = 0.f;
-    }
-    if (cell < cd.ncells) {
-      const int gx = cell % cd.Mx, gy = (cell / cd.Mx) % cd.My, gz = cell / (cd.Mx * cd.My);
-      const int nx = gx + k % 3 - 1, ny = gy + (k / 3) % 3 - 1, nz = gz + k / 9 - 1;
-      // the slice's sub-column: x and z ranges in code units
-      const int isx = item.x % sub, isz = (item.x / sub) % sub;
-      const float ix0 = (gx * sub + isx) * cd.HCsx, iz0 = (gz * sub + isz) * cd.HCsz;
-      // y range of the slice: its first particle (lane 0, u = 0) and its last one
-      const float ys0 = __shfl_sync(0xFFFFFFFFu, I[0].p.y, 0);
-      const float ys1 = __ldg(&pm[last].y);
-      // origin of the scaled coordinates: the slice's first particle (near every pair's ends, so
-      // the differences keep the precision of code-unit differences)
-      const float ox = __shfl_sync(0xFFFFFFFFu, I[0].p.x, 0), oz = __shfl_sync(0xFFFFFFFFu, I[0].p.z, 0);
-#pragma unroll
-      for (int u = 0; u < SLOT_IPL; ++u) {
-        I[u].p.x = (I[u].p.x - ox) * sc;
-        I[u].p.y = (I[u].p.y - ys0) * sc;
-        I[u].p.z = (I[u].p.z - oz) * sc;
-      }
-      if (nx >= 0 && ny >= 0 && nz >= 0 && nx < cd.Mx && ny < cd.My && nz < cd.Mz)
-      for (int qs = 0; qs < sub2; ++qs) {
-        const int jsx = qs % sub, jsz = qs / sub;
-        const float jx0 = (nx * sub + jsx) * cd.HCsx, jz0 = (nz * sub + jsz) * cd.HCsz;
-        const float gxs = fmaxf(fmaxf(jx0 - (ix0 + cd.HCsx), ix0 - (jx0 + cd.HCsx)) - gap_margin, 0.f);
-        const float gzs = fmaxf(fmaxf(jz0 - (iz0 + cd.HCsz), iz0 - (jz0 + cd.HCsz)) - gap_margin, 0.f);
-        const float g2 = gxs * gxs + gzs * gzs;
-        if (g2 >= pp.re2) continue;
-        // a pair in range has |dy|^2 < re^2 - (its x-z distance)^2 <= re^2 - g2: the y window
-        // of this sub-column is the chord of the cutoff sphere at the sub-column's x-z gap, widened
-        // by 1e-5 of the coordinates' size against float rounding of the comparisons
-        const float h = sqrtf(pp.re2 - g2) + 1e-5f * (1.f + fabsf(ys1));
-        const int cn = (nx + ny * cd.Mx + nz * cd.Mx * cd.My) * sub2 + qs;
-        int b = cell_start[cn];
-        int e = cell_start[cn + 1];
-        if (pp.ysort && e > b) {
-          b = warp_y_bound<false>(pm, b, e, ys0 - h, lane);
-          e = warp_y_bound<true>(pm, b, e, ys1 + h, lane);
-        }
-        for (int j0 = b; j0 < e; j0 += 32) {
-          const int jj = j0 + lane;
-          float4 qj = jj < e ? pm[jj] : make_float4(3.0e30f, 3.0e30f, 3.0e30f, 0.f);
-          qj.x = (qj.x - ox) * sc;
-          qj.y = (qj.y - ys0) * sc;
-          qj.z = (qj.z - oz) * sc;
-          jbuf[warp][lane] = qj;
-          __syncwarp();
-          const int cnt = min(32, e - j0);
-#pragma unroll
-          for (int u = 0; u < SLOT_IPL; ++u) I[u].px = I[u].py = I[u].pz = 0.f;
-#pragma unroll 4
-          for (int s = 0; s < cnt; ++s) {
-            const float4 q = jbuf[warp][s];
-#pragma unroll
-            for (int u = 0; u < SLOT_IPL; ++u) slot_pair<EQM>(I[u], q, tab_base);
-          }
-          __syncwarp();
-#pragma unroll
-          for (int u = 0; u < SLOT_IPL; ++u) {
-            kahan_add(I[u].sx, I[u].cx, I[u].px);
-            kahan_add(I[u].sy, I[u].cy, I[u].py);
-            kahan_add(I[u].sz, I[u].cz, I[u].pz);
-          }
-        }
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < SLOT_IPL; ++u) {
-      const int i = item.y + 32 * u + lane;
-      if (i < cend) slots[(size_t)k * n + i] = make_float4(I[u].sx, I[u].sy, I[u].sz, 0.f);
-    }
+    if (it >= nall) break;
+    if (listed && slot_heavy(cell_start, cd, items[it / NNB], (int)(it % NNB))) continue;
+    slot_unit<EQM, false>(c, it, jbuf, part, tab_base, lane, warp);
   }
 }
 
@@ -474,13 +561,35 @@ __global__ void item_build_kernel(const int* __restrict__ cell_start, const u32*
   for (int s = b; s < e; s += slice) items[o++] = make_int2(c, s);
 }
 
+// Lists the heavy units (slot_heavy): one thread per item, its 27 neighbour cells.  counter[2]
+// counts them; only the first `cap` are stored (beyond, the table pass lists none as heavy).
+__global__ void plan_heavy_kernel(const int* __restrict__ cell_start, const int2* __restrict__ items,
+                                  const u32* __restrict__ nitems_p, ChainDimsP cd,
+                                  u32* __restrict__ heavy, u32 cap, u32* __restrict__ counter,
+                                  const int* stop) {
+  if (*stop) return;
+  const u32 item = blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= *nitems_p) return;
+  const int2 it = items[item];
+  for (int k = 0; k < NNB; ++k) {
+    if (!slot_heavy(cell_start, cd, it, k)) continue;
+    const u32 h = atomicAdd(&counter[2], 1u);
+    if (h < cap) heavy[h] = item * NNB + k;
+  }
+}
+
+int slot_heavy_capacity(int nitems_max) {
+  const long long units = (long long)nitems_max * NNB;
+  return (int)(units < (1 << 22) ? units : (1 << 22));
+}
+
 int exclusive_scan(const u32* in, u32* out, int n, u32* total, u32* scratch, cudaStream_t st);
 
 int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const int* cell_start,
                 const ChainDims& chd, u32* item_cnt, u32* item_off, u32* scan_tmp, u32* nitems, int2* items,
-                u32* counter, const PairParams& pp, const float* table, const StepParams& sp,
-                float kick, int drift, int kdk, float4* pm_out, float4* vi_out, float4* acc_out,
-                unsigned long long* npairs, int* stop, int num_sms, cudaEvent_t ev_pair,
+                int nitems_max, u32* heavy, u32* counter, const PairParams& pp, const float* table,
+                const StepParams& sp, float kick, int drift, int kdk, float4* pm_out, float4* vi_out,
+                float4* acc_out, unsigned long long* npairs, int* stop, int num_sms, cudaEvent_t ev_pair,
                 cudaStream_t st, int equal_mass, float4* slots, int n) {
   const int ncells = chd.Mx * chd.My * chd.Mz;
   const int ntot = ncells * chd.sub * chd.sub + 1;  // sub-columns + the bucket outside the mesh
@@ -490,12 +599,16 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
   int rc = exclusive_scan(item_cnt, item_off, ntot, nitems, scan_tmp, st);
   if (rc) return rc;
   item_build_kernel<<<(ntot + 255) / 256, 256, 0, st>>>(cell_start, item_off, ntot, items, slice, stop);
-  PMGB_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(u32), st));
+  PMGB_CUDA_TRY(cudaMemsetAsync(counter, 0, 3 * sizeof(u32), st));
   if (npairs) PMGB_CUDA_TRY(cudaMemsetAsync(npairs, 0, sizeof(unsigned long long), st));
-  if (ev_pair) PMGB_CUDA_TRY(cudaEventRecord(ev_pair, st));
   ChainDimsP cd{chd.Mx, chd.My, chd.Mz, ncells, chd.sub, chd.HCsx, chd.HCsz};
+  const u32 heavy_cap = (u32)slot_heavy_capacity(nitems_max);
+  if (slotted && nitems_max > 0)
+    plan_heavy_kernel<<<(nitems_max + 255) / 256, 256, 0, st>>>(cell_start, items, nitems, cd, heavy, heavy_cap,
+                                                                counter, stop);
+  if (ev_pair) PMGB_CUDA_TRY(cudaEventRecord(ev_pair, st));
   const dim3 grid(num_sms * 8), block(PAIR_THREADS);
-  if (slotted) {  // 64 KB + staging of dynamic shared memory (set for the current device)
+  if (slotted) {  // table, staging and partial sums: 86.5 KB of dynamic shared memory
     PMGB_CUDA_TRY(cudaFuncSetAttribute(pair_slot_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SLOT_SMEM));
     PMGB_CUDA_TRY(cudaFuncSetAttribute(pair_slot_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SLOT_SMEM));
   }
@@ -505,10 +618,10 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
   if (slotted) {
     if (equal_mass)
       pair_slot_kernel<true><<<num_sms * 2, SLOT_THREADS, SLOT_SMEM, st>>>(
-          pm, n, cell_start, items, nitems, counter, cd, pp, table, slots, stop);
+          pm, n, cell_start, items, nitems, heavy, heavy_cap, counter, cd, pp, table, slots, stop);
     else
       pair_slot_kernel<false><<<num_sms * 2, SLOT_THREADS, SLOT_SMEM, st>>>(
-          pm, n, cell_start, items, nitems, counter, cd, pp, table, slots, stop);
+          pm, n, cell_start, items, nitems, heavy, heavy_cap, counter, cd, pp, table, slots, stop);
     if (n > 0)
       pair_epilogue_kernel<<<(n + 255) / 256, 256, 0, st>>>(pm, vi, acc_pm, slots, n, sp, kick, drift,
                                                             kdk, pm_out, vi_out, acc_out, stop);
