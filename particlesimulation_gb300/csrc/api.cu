@@ -636,7 +636,7 @@ int p3m_create_internal(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out,
   // units, and its 27 partial-force slots per particle
   q->nitems_max = (int)((size_t)pm->n / 32 + ntot + 32);
   if ((rc = dalloc(&q->cell_start, ntot + 1)) || (rc = dalloc(&q->item_cnt, ntot)) ||
-      (rc = dalloc(&q->item_off, ntot)) || (rc = dalloc(&q->nitems, 1)) || (rc = dalloc(&q->counter, 3)) ||
+      (rc = dalloc(&q->item_off, ntot)) || (rc = dalloc(&q->nitems, 1)) || (rc = dalloc(&q->counter, (size_t)slot_counter_words())) ||
       (rc = dalloc(&q->scan_tmp, (size_t)scan_scratch_words((int)ntot))) ||
       (rc = dalloc(&q->items, (size_t)q->nitems_max)) ||
       (rc = dalloc(&q->heavy, (size_t)slot_heavy_capacity(q->nitems_max))) ||

@@ -11,6 +11,7 @@ int radix_sort_pairs(u64** keys, u32** vals, u64** keys_alt, u32** vals_alt, u32
                      int nbits, cudaStream_t st);
 int scan_scratch_words(int n);   // size of exclusive_scan's scratch buffer
 int slot_heavy_capacity(int nitems_max);  // entries of the pair pass's heavy-unit list
+int slot_counter_words();                 // words of the pair pass's counter buffer
 int exclusive_scan(const u32* in, u32* out, int n, u32* total, u32* scratch, cudaStream_t st);
 int launch_chain_keys(const float4* pm, const float4* vi, int n, ChainDims c, int ysort,
                       const int* stop, u64* keys, u32* vals, cudaStream_t st);

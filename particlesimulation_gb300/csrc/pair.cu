@@ -243,8 +243,10 @@ constexpr int SLOT_THREADS = 512;
 constexpr int SLOT_WARPS = SLOT_THREADS / 32;
 // staging (SLOT_WARPS x 32 float4) + CTA partial sums (SLOT_WARPS x SLOT_SLICE float4) + table
 constexpr int SLOT_SMEM = SLOT_WARPS * 32 * 16 + SLOT_WARPS * SLOT_SLICE * 16 + SLOT_TAB * SLOT_REP * 8;
-// Cells with at least this many particles: their slices' units are taken by whole CTAs.
-constexpr int SLOT_HEAVY_POP = 16384;
+// Units whose estimated cost reaches 1/SLOT_HEAVY_DIV of a warp's share of the pass (and at
+// least SLOT_HEAVY_MIN) are taken by whole CTAs.
+constexpr int SLOT_HEAVY_DIV = 4;
+constexpr unsigned long long SLOT_HEAVY_MIN = 64ull * 1024;
 
 struct SlotI {
   float4 p;
@@ -299,19 +301,22 @@ __device__ __forceinline__ int warp_y_bound(const float4* __restrict__ pm, int l
   return lo + __popc(__ballot_sync(0xFFFFFFFFu, below));
 }
 
-// A unit is heavy when its neighbour cell holds at least SLOT_HEAVY_POP particles: its slice
-// then meets up to that many candidates per particle (a whole warp's share of the pass on the
-// bulge of the disk workloads), so whole CTAs take the heavy units first.
-__device__ __forceinline__ bool slot_heavy(const int* __restrict__ cell_start, const ChainDimsP& cd,
-                                           int2 item, int k) {
+// Estimated time of a unit for its warp: SLOT_SLICE times the neighbour cell's particles (the
+// lanes run every candidate of the window whether or not all of them hold a particle, so a
+// partial slice costs as much as a full one).  On the disk workloads a unit against the bulge
+// can come close to a warp's whole share of the pass, and a warp holding one at the end leaves
+// the GPU idle.
+__device__ __forceinline__ unsigned long long slot_cost(const int* __restrict__ cell_start,
+                                                        const ChainDimsP& cd, int2 item, int k) {
   const int sub2 = cd.sub * cd.sub;
   const int cell = item.x / sub2;
-  if (cell >= cd.ncells) return false;
+  if (cell >= cd.ncells) return 0;
   const int gx = cell % cd.Mx, gy = (cell / cd.Mx) % cd.My, gz = cell / (cd.Mx * cd.My);
   const int nx = gx + k % 3 - 1, ny = gy + (k / 3) % 3 - 1, nz = gz + k / 9 - 1;
-  if (nx < 0 || ny < 0 || nz < 0 || nx >= cd.Mx || ny >= cd.My || nz >= cd.Mz) return false;
+  if (nx < 0 || ny < 0 || nz < 0 || nx >= cd.Mx || ny >= cd.My || nz >= cd.Mz) return 0;
   const int nb = nx + ny * cd.Mx + nz * cd.Mx * cd.My;
-  return __ldg(&cell_start[(nb + 1) * sub2]) - __ldg(&cell_start[nb * sub2]) >= SLOT_HEAVY_POP;
+  return (unsigned long long)SLOT_SLICE *
+         (unsigned long long)(__ldg(&cell_start[(nb + 1) * sub2]) - __ldg(&cell_start[nb * sub2]));
 }
 
 // Per-launch constants of the table pass.
@@ -446,10 +451,11 @@ __device__ __forceinline__ void slot_unit(const SlotCtx& c, u32 it, float4 (*jbu
   }
 }
 
-// The heavy units listed by plan_heavy_kernel (heavy[0, counter[2])) are taken first, each by a
-// whole CTA (counter[0]), so that no single warp is left with a unit of tens of thousands of
-// candidates per particle while the others idle; then every warp takes the other units one at a
-// time (counter[1]).  If the list overflowed its capacity, no unit is treated as heavy.
+// The heavy units listed by plan_heavy_kernel (heavy[0, counter[2]), cost at least the
+// threshold in counter[6..7]) are taken first, each by a whole CTA (counter[0]), so that no
+// single warp is left with a unit of tens of thousands of candidates per particle while the
+// others idle; then every warp takes the other units one at a time (counter[1]).  If the list
+// overflowed its capacity, no unit is treated as heavy.
 template <bool EQM>
 __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
     const float4* __restrict__ pm, int n, const int* __restrict__ cell_start,
@@ -491,6 +497,7 @@ __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
   const u32 nlisted = __ldcg(&counter[2]);
   const bool listed = nlisted <= heavy_cap;  // the heavy units are all in the list
   const u32 nheavy = listed ? nlisted : 0u;
+  const unsigned long long thr = __ldcg(reinterpret_cast<const unsigned long long*>(counter + 6));
   for (;;) {
     if (threadIdx.x == 0) s_unit = atomicAdd(&counter[0], 1u);
     __syncthreads();
@@ -504,7 +511,7 @@ __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
     if (lane == 0) it = atomicAdd(&counter[1], 1u);
     it = __shfl_sync(0xFFFFFFFFu, it, 0);
     if (it >= nall) break;
-    if (listed && slot_heavy(cell_start, cd, items[it / NNB], (int)(it % NNB))) continue;
+    if (listed && slot_cost(cell_start, cd, items[it / NNB], (int)(it % NNB)) >= thr) continue;
     slot_unit<EQM, false>(c, it, jbuf, part, tab_base, lane, warp);
   }
 }
@@ -561,22 +568,48 @@ __global__ void item_build_kernel(const int* __restrict__ cell_start, const u32*
   for (int s = b; s < e; s += slice) items[o++] = make_int2(c, s);
 }
 
-// Lists the heavy units (slot_heavy): one thread per item, its 27 neighbour cells.  counter[2]
-// counts them; only the first `cap` are stored (beyond, the table pass lists none as heavy).
+// counter words of the table pass: [0] CTA units taken, [1] warp units taken, [2] heavy units
+// listed, [4..5] u64 total estimated cost, [6..7] u64 heavy threshold.
+constexpr int SLOT_COUNTER_WORDS = 8;
+
+// Total estimated cost of all units (one thread per item, its 27 neighbour cells).
+__global__ void plan_cost_kernel(const int* __restrict__ cell_start, const int2* __restrict__ items,
+                                 const u32* __restrict__ nitems_p, ChainDimsP cd, u32* __restrict__ counter,
+                                 const int* stop) {
+  if (*stop) return;
+  const u32 item = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long s = 0;
+  if (item < *nitems_p) {
+    const int2 it = items[item];
+    for (int k = 0; k < NNB; ++k) s += slot_cost(cell_start, cd, it, k);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
+  if ((threadIdx.x & 31) == 0 && s) atomicAdd(reinterpret_cast<unsigned long long*>(counter + 4), s);
+}
+
+// Sets the threshold (a 1/SLOT_HEAVY_DIV share of one of `warps` warps, at least SLOT_HEAVY_MIN)
+// and lists the units at or above it: heavy[0, min(counter[2], cap)).  Beyond `cap` entries
+// the table pass treats no unit as heavy.
 __global__ void plan_heavy_kernel(const int* __restrict__ cell_start, const int2* __restrict__ items,
                                   const u32* __restrict__ nitems_p, ChainDimsP cd,
                                   u32* __restrict__ heavy, u32 cap, u32* __restrict__ counter,
-                                  const int* stop) {
+                                  unsigned long long warps, const int* stop) {
   if (*stop) return;
+  const unsigned long long total = __ldcg(reinterpret_cast<const unsigned long long*>(counter + 4));
+  const unsigned long long t = total / (warps * SLOT_HEAVY_DIV);
+  const unsigned long long thr = t > SLOT_HEAVY_MIN ? t : SLOT_HEAVY_MIN;
   const u32 item = blockIdx.x * blockDim.x + threadIdx.x;
+  if (item == 0) *reinterpret_cast<unsigned long long*>(counter + 6) = thr;
   if (item >= *nitems_p) return;
   const int2 it = items[item];
   for (int k = 0; k < NNB; ++k) {
-    if (!slot_heavy(cell_start, cd, it, k)) continue;
+    if (slot_cost(cell_start, cd, it, k) < thr) continue;
     const u32 h = atomicAdd(&counter[2], 1u);
     if (h < cap) heavy[h] = item * NNB + k;
   }
 }
+
+int slot_counter_words() { return SLOT_COUNTER_WORDS; }
 
 int slot_heavy_capacity(int nitems_max) {
   const long long units = (long long)nitems_max * NNB;
@@ -599,13 +632,16 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
   int rc = exclusive_scan(item_cnt, item_off, ntot, nitems, scan_tmp, st);
   if (rc) return rc;
   item_build_kernel<<<(ntot + 255) / 256, 256, 0, st>>>(cell_start, item_off, ntot, items, slice, stop);
-  PMGB_CUDA_TRY(cudaMemsetAsync(counter, 0, 3 * sizeof(u32), st));
+  PMGB_CUDA_TRY(cudaMemsetAsync(counter, 0, SLOT_COUNTER_WORDS * sizeof(u32), st));
   if (npairs) PMGB_CUDA_TRY(cudaMemsetAsync(npairs, 0, sizeof(unsigned long long), st));
   ChainDimsP cd{chd.Mx, chd.My, chd.Mz, ncells, chd.sub, chd.HCsx, chd.HCsz};
   const u32 heavy_cap = (u32)slot_heavy_capacity(nitems_max);
-  if (slotted && nitems_max > 0)
-    plan_heavy_kernel<<<(nitems_max + 255) / 256, 256, 0, st>>>(cell_start, items, nitems, cd, heavy, heavy_cap,
-                                                                counter, stop);
+  if (slotted && nitems_max > 0) {
+    const int pb = (nitems_max + 255) / 256;
+    plan_cost_kernel<<<pb, 256, 0, st>>>(cell_start, items, nitems, cd, counter, stop);
+    plan_heavy_kernel<<<pb, 256, 0, st>>>(cell_start, items, nitems, cd, heavy, heavy_cap, counter,
+                                          (unsigned long long)num_sms * 2 * SLOT_WARPS, stop);
+  }
   if (ev_pair) PMGB_CUDA_TRY(cudaEventRecord(ev_pair, st));
   const dim3 grid(num_sms * 8), block(PAIR_THREADS);
   if (slotted) {  // table, staging and partial sums: 86.5 KB of dynamic shared memory
@@ -616,6 +652,7 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
                        drift, kdk, pm_out, vi_out, acc_out, npairs, stop
   int launches = 3;  // item count, item build, pair pass (the scan counts itself)
   if (slotted) {
+    if (nitems_max > 0) launches += 2;  // the two planning kernels
     if (equal_mass)
       pair_slot_kernel<true><<<num_sms * 2, SLOT_THREADS, SLOT_SMEM, st>>>(
           pm, n, cell_start, items, nitems, heavy, heavy_cap, counter, cd, pp, table, slots, stop);
