@@ -392,12 +392,15 @@ __device__ __forceinline__ void slot_unit(const SlotCtx& c, u32 it, float4 (*jbu
         b = warp_y_bound<false>(c.pm, b, e, ys0 - h, lane);
         e = warp_y_bound<true>(c.pm, b, e, ys1 + h, lane);
       }
-      for (int j0 = b; j0 < e; j0 += 32) {
-        if (COOP) {
-          const bool mine = (chunk & (SLOT_WARPS - 1)) == warp;
-          ++chunk;
-          if (!mine) continue;
-        }
+      // COOP: this warp's chunks of the window are c = first, first + SLOT_WARPS, ... where
+      // chunk + first = warp (mod SLOT_WARPS)
+      int j0 = b, jstep = 32;
+      if (COOP) {
+        j0 = b + 32 * ((warp - chunk) & (SLOT_WARPS - 1));
+        jstep = 32 * SLOT_WARPS;
+        chunk += (e - b + 31) >> 5;
+      }
+      for (; j0 < e; j0 += jstep) {
         const int jj = j0 + lane;
         float4 qj = jj < e ? c.pm[jj] : make_float4(3.0e30f, 3.0e30f, 3.0e30f, 0.f);
         qj.x = (qj.x - ox) * sc;
@@ -452,10 +455,11 @@ __device__ __forceinline__ void slot_unit(const SlotCtx& c, u32 it, float4 (*jbu
 }
 
 // The heavy units listed by plan_heavy_kernel (heavy[0, counter[2]), cost at least the
-// threshold in counter[6..7]) are taken first, each by a whole CTA (counter[0]), so that no
-// single warp is left with a unit of tens of thousands of candidates per particle while the
-// others idle; then every warp takes the other units one at a time (counter[1]).  If the list
-// overflowed its capacity, no unit is treated as heavy.
+// threshold thr in counter[6..7]) are taken first, each by a whole CTA (counter[0]), so that
+// no single warp is left with a unit of tens of thousands of candidates per particle while the
+// others idle; then every warp takes the medium units (cost in [thr / 4, thr), listed from the
+// far end of the same buffer, counter[1]), then the rest in unit order (counter[8]).  If the
+// lists overflowed the buffer, every unit is taken by the last loop.
 template <bool EQM>
 __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
     const float4* __restrict__ pm, int n, const int* __restrict__ cell_start,
@@ -494,9 +498,9 @@ __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
   // least the cutoff (with a margin far above the rounding of the sub-column assignment)
   const SlotCtx c{pm, cell_start, items, slots, n, cd, pp.re2, sc, 1e-3f * fminf(cd.HCsx, cd.HCsz), pp.ysort};
   const u32 nall = *nitems_p * NNB;  // every slice once per neighbour cell
-  const u32 nlisted = __ldcg(&counter[2]);
-  const bool listed = nlisted <= heavy_cap;  // the heavy units are all in the list
-  const u32 nheavy = listed ? nlisted : 0u;
+  const u32 nh = __ldcg(&counter[2]), nm = __ldcg(&counter[3]);
+  const bool listed = (unsigned long long)nh + nm <= heavy_cap;  // both lists complete
+  const u32 nheavy = listed ? nh : 0u, nmedium = listed ? nm : 0u;
   const unsigned long long thr = __ldcg(reinterpret_cast<const unsigned long long*>(counter + 6));
   for (;;) {
     if (threadIdx.x == 0) s_unit = atomicAdd(&counter[0], 1u);
@@ -507,11 +511,18 @@ __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
     slot_unit<EQM, true>(c, __ldg(&heavy[h]), jbuf, part, tab_base, lane, warp);
   }
   for (;;) {
+    u32 m = 0;
+    if (lane == 0) m = atomicAdd(&counter[1], 1u);
+    m = __shfl_sync(0xFFFFFFFFu, m, 0);
+    if (m >= nmedium) break;
+    slot_unit<EQM, false>(c, __ldg(&heavy[heavy_cap - 1 - m]), jbuf, part, tab_base, lane, warp);
+  }
+  for (;;) {
     u32 it = 0;
-    if (lane == 0) it = atomicAdd(&counter[1], 1u);
+    if (lane == 0) it = atomicAdd(&counter[8], 1u);
     it = __shfl_sync(0xFFFFFFFFu, it, 0);
     if (it >= nall) break;
-    if (listed && slot_cost(cell_start, cd, items[it / NNB], (int)(it % NNB)) >= thr) continue;
+    if (listed && slot_cost(cell_start, cd, items[it / NNB], (int)(it % NNB)) >= thr / 4) continue;
     slot_unit<EQM, false>(c, it, jbuf, part, tab_base, lane, warp);
   }
 }
@@ -568,9 +579,10 @@ __global__ void item_build_kernel(const int* __restrict__ cell_start, const u32*
   for (int s = b; s < e; s += slice) items[o++] = make_int2(c, s);
 }
 
-// counter words of the table pass: [0] CTA units taken, [1] warp units taken, [2] heavy units
-// listed, [4..5] u64 total estimated cost, [6..7] u64 heavy threshold.
-constexpr int SLOT_COUNTER_WORDS = 8;
+// counter words of the table pass: [0] heavy units taken (by CTAs), [1] medium units taken,
+// [2] heavy units listed, [3] medium units listed, [4..5] u64 total estimated cost, [6..7] u64
+// heavy threshold, [8] other units taken.
+constexpr int SLOT_COUNTER_WORDS = 10;
 
 // Total estimated cost of all units (one thread per item, its 27 neighbour cells).
 __global__ void plan_cost_kernel(const int* __restrict__ cell_start, const int2* __restrict__ items,
@@ -587,9 +599,10 @@ __global__ void plan_cost_kernel(const int* __restrict__ cell_start, const int2*
   if ((threadIdx.x & 31) == 0 && s) atomicAdd(reinterpret_cast<unsigned long long*>(counter + 4), s);
 }
 
-// Sets the threshold (a 1/SLOT_HEAVY_DIV share of one of `warps` warps, at least SLOT_HEAVY_MIN)
-// and lists the units at or above it: heavy[0, min(counter[2], cap)).  Beyond `cap` entries
-// the table pass treats no unit as heavy.
+// Sets the threshold thr (a 1/SLOT_HEAVY_DIV share of one of `warps` warps, at least
+// SLOT_HEAVY_MIN) and lists the heavy units (cost >= thr) from the front of `heavy`, the medium
+// ones (thr / 4 <= cost < thr) from its back.  If the two lists do not fit in `cap` entries
+// together, the table pass uses neither.
 __global__ void plan_heavy_kernel(const int* __restrict__ cell_start, const int2* __restrict__ items,
                                   const u32* __restrict__ nitems_p, ChainDimsP cd,
                                   u32* __restrict__ heavy, u32 cap, u32* __restrict__ counter,
@@ -603,9 +616,14 @@ __global__ void plan_heavy_kernel(const int* __restrict__ cell_start, const int2
   if (item >= *nitems_p) return;
   const int2 it = items[item];
   for (int k = 0; k < NNB; ++k) {
-    if (slot_cost(cell_start, cd, it, k) < thr) continue;
-    const u32 h = atomicAdd(&counter[2], 1u);
-    if (h < cap) heavy[h] = item * NNB + k;
+    const unsigned long long cost = slot_cost(cell_start, cd, it, k);
+    if (cost >= thr) {
+      const u32 h = atomicAdd(&counter[2], 1u);
+      if (h < cap) heavy[h] = item * NNB + k;
+    } else if (cost >= thr / 4) {
+      const u32 m = atomicAdd(&counter[3], 1u);
+      if (m < cap) heavy[cap - 1 - m] = item * NNB + k;
+    }
   }
 }
 
