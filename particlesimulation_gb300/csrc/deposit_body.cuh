@@ -88,7 +88,8 @@ __device__ __forceinline__ int block_min(int v, int* red) {
 }
 __device__ __forceinline__ int block_max(int v, int* red) { return -block_min(-v, red); }
 
-template <int IS, int PPT>
+// tile: TILE u64 cells of shared memory.
+template <int IS, int PPT, int TILE = DEP_TILE>
 __device__ __forceinline__ void deposit_block(const float4* __restrict__ pm, int base, int n,
                                               const MeshDims& m, float scale, u64* __restrict__ rho,
                                               u64* tile, int* red) {
@@ -114,7 +115,7 @@ __device__ __forceinline__ void deposit_block(const float4* __restrict__ pm, int
   const int ey = mxy - mny + Stencil<IS>::lo + Stencil<IS>::hi + 1;
   const int ez = mxz - mnz + Stencil<IS>::lo + Stencil<IS>::hi + 1;
   const long long vol = (long long)ex * ey * ez;
-  const bool use_tile = vol <= DEP_TILE && ex <= m.nx && ey <= m.ny && ez <= m.nz;
+  const bool use_tile = vol <= TILE && ex <= m.nx && ey <= m.ny && ez <= m.nz;
   const size_t sxy = (size_t)m.nx * m.ny;
 
   if (use_tile) {
@@ -129,12 +130,16 @@ __device__ __forceinline__ void deposit_block(const float4* __restrict__ pm, int
       });
     }
     __syncthreads();
-    for (int c = threadIdx.x; c < (int)vol; c += DEP_THREADS) {
-      u64 v = tile[c];
-      if (v == 0ull) continue;
-      int x = ox + c % ex, y = oy + (c / ex) % ey, z = oz + c / (ex * ey);
-      fx_add_global(&rho[(size_t)wrapi(z, m.nz) * sxy + (size_t)wrapi(y, m.ny) * m.nx + wrapi(x, m.nx)],
-                    (long long)v);
+    // one mesh row (y, z) of the tile per warp, x across the lanes
+    const int lane = threadIdx.x & 31;
+    for (int r = threadIdx.x >> 5; r < ey * ez; r += DEP_THREADS / 32) {
+      const int tz = r / ey, ty = r - tz * ey;
+      u64* row = rho + (size_t)wrapi(oz + tz, m.nz) * sxy + (size_t)wrapi(oy + ty, m.ny) * m.nx;
+      const u64* trow = tile + r * ex;
+      for (int tx = lane; tx < ex; tx += 32) {
+        const u64 v = trow[tx];
+        if (v != 0ull) fx_add_global(&row[wrapi(ox + tx, m.nx)], (long long)v);
+      }
     }
   } else {
 #pragma unroll
