@@ -347,26 +347,34 @@ __global__ void brick_keys_kernel(const float4* __restrict__ pm, int n, MeshDims
   vals[i] = (u32)i;
 }
 
-// Permute particles into sorted order.  For the P3M order also records cell start offsets
-// (cell_start[c] = first sorted slot of cell c; cell_start[ncells + 1] = n).
-__global__ void gather_kernel(const u64* __restrict__ keys, const u32* __restrict__ vals, int n,
-                              const float4* __restrict__ pm_in, const float4* __restrict__ vi_in,
-                              float4* __restrict__ pm_out, float4* __restrict__ vi_out,
-                              int* __restrict__ cell_start, int ncells_total,
-                              const int* __restrict__ stop) {
+// Permute particles into sorted order.
+__global__ void gather_kernel(const u32* __restrict__ vals, int n, const float4* __restrict__ pm_in,
+                              const float4* __restrict__ vi_in, float4* __restrict__ pm_out,
+                              float4* __restrict__ vi_out, const int* __restrict__ stop) {
   if (stop && *stop) return;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   u32 s = vals[i];
   pm_out[i] = pm_in[s];
   vi_out[i] = vi_in[s];
-  if (cell_start) {
-    int c = (int)(keys[i] >> 32);
-    int prev = i == 0 ? -1 : (int)(keys[i - 1] >> 32);
-    for (int cc = prev + 1; cc <= c; ++cc) cell_start[cc] = i;
-    if (i == n - 1)
-      for (int cc = c + 1; cc <= ncells_total; ++cc) cell_start[cc] = n;
+}
+
+// Cell start offsets of the P3M order: cell_start[c] = first sorted slot whose cell (key >> 32)
+// is at least c, for c = 0 .. ncells_total (so cell_start[ncells_total] = n when every key is
+// below it).  One binary search per cell, so long runs of empty cells cost no thread more than
+// the others.
+__global__ void cell_start_kernel(const u64* __restrict__ keys, int n, int* __restrict__ cell_start,
+                                  int ncells_total, const int* __restrict__ stop) {
+  if (stop && *stop) return;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c > ncells_total) return;
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if ((int)(__ldg(&keys[mid]) >> 32) < c) lo = mid + 1;
+    else hi = mid;
   }
+  cell_start[c] = lo;
 }
 
 __global__ void fill_int_kernel(int* p, int n, int v) {
@@ -410,10 +418,11 @@ int launch_gather(const u64* keys, const u32* vals, int n, const float4* pm_in,
     }
     return PMGB_OK;
   }
-  gather_kernel<<<(n + 255) / 256, 256, 0, st>>>(keys, vals, n, pm_in, vi_in, pm_out, vi_out,
-                                                 cell_start, ncells_total, stop);
+  gather_kernel<<<(n + 255) / 256, 256, 0, st>>>(vals, n, pm_in, vi_in, pm_out, vi_out, stop);
+  if (cell_start)
+    cell_start_kernel<<<(ncells_total + 256) / 256, 256, 0, st>>>(keys, n, cell_start, ncells_total, stop);
   PMGB_LAUNCH_CHECK();
-  count_launches(1);
+  count_launches(cell_start ? 2 : 1);
   return PMGB_OK;
 }
 
