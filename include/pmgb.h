@@ -74,7 +74,7 @@ typedef struct pmgb_pm_config {
   float particle_diameter; /* original units */
   pmgb_external_field ext;
   /* PM-only runs re-sort particles every `sort_interval` steps (results do not depend on the
-   * order; only locality does).  0 = default (8). */
+   * order; only locality does).  0 = default (16). */
   int sort_interval;
   /* 0: the reference's isolated setup (particles must stay in [0, box]; leaving it stops a
    * run, PMGB_EESCAPED).  1: periodic box equal to the mesh: positions wrap after each drift and
