@@ -6,13 +6,20 @@
 //   pmgb_demos <option> [output dir]
 //
 // Options: galaxy-sim-pm, galaxy-sim-p3m, galaxy-collision-sim-pm, galaxy-collision-sim-p3m,
-// cluster-sim-pm, cluster-sim-p3m, galaxy-sim-pm-timing, galaxy-sim-p3m-timing.
+// cluster-sim-pm, cluster-sim-p3m, galaxy-sim-pm-timing, galaxy-sim-p3m-timing, and the PM field
+// sweeps anisotropy, finite-diff-err, assignment-schemes, poor-man-vs-laplacian, pm-optimal,
+// pm-optimal-var-diameter, pm-optimal-assignments.  Not provided: pm-accuracy-soft /
+// pm-accuracy-no-soft (meshes of 2 Ng x 2 Ng x Ng points for Ng = 30 .. 70, none a power of two,
+// which the transforms here require) and p3m-accuracy-assignments / p3m-accuracy-shapes (their
+// reference forces come from the direct-sum PP integrator, which is not part of this path); the
+// Barnes-Hut scenarios are out of scope as well.
 // Differences from the reference's scenarios, all deliberate: the external field is passed as a
 // description (the GPU path has no host callbacks); galaxy-sim-p3m uses the reference's CPU
 // settings (S1-optimal influence function, a = 3H), which its CUDA build replaced by the
 // discrete Laplacian; cluster-sim-p3m runs P3M (the reference builds the P3MMethod and then
 // runs the plain PM method).
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <functional>
 #include <iostream>
@@ -150,6 +157,109 @@ void plummer(const std::string& out, bool p3mRun) {
   }
 }
 
+// The PM field sweeps (anisotropy, finiteDiffRelError, assignmentSchemes, poorLaplace,
+// pmOptimal, pmOptimalVaryingDiameter, pmOptimalAssignments; source/demos.cpp:109-591): one
+// particle of mass 1 at `center` and 399 massless tracers every 0.075 along `dir`, 64 x 64 x 32
+// mesh over a 60 x 60 x 30 box (H = 60 / 32), G = 4.5e-3, DT = 1, one iteration with the
+// positions and the field (the acceleration each tracer feels) recorded.
+std::vector<Vec3> linearSpacing(int n, float dx, Vec3 center, Vec3 dir) {
+  std::vector<Vec3> state(2 * size_t(n), Vec3{});
+  for (int i = 0; i < n; ++i)
+    state[i] = v3(center.x + i * dx * dir.x, center.y + i * dx * dir.y, center.z + i * dx * dir.z);
+  return state;
+}
+
+void fieldSweep(const std::string& out, const char* positionsFile, const char* fieldFile, Vec3 center,
+                Vec3 dir, InterpolationScheme is, FiniteDiffScheme fds, GreensFunction gf,
+                float particleDiameter) {
+  const int n = 400, simLength = 1;
+  const float G = 4.5e-3f;
+  std::vector<float> masses(n, 0.0f);
+  masses[0] = 1.0f;
+  const auto gridPoints = std::make_tuple(64, 64, 32);
+  const auto box = std::make_tuple(60.0f, 60.0f, 30.0f);
+  const float H = std::get<0>(box) / (std::get<0>(gridPoints) / 2), DT = 1;
+  StateRecorder stateRecorder(n, simLength + 1, out, positionsFile, "", "", "", "", fieldFile);
+  PMMethodGPU pm(linearSpacing(n, 0.075f, center, dir), masses, box, ExternalField::none(), H, DT, G, is,
+                 fds, gf, particleDiameter, gridPoints);
+  pm.run(stateRecorder, simLength, false /*diagnostics*/, true /*field*/);
+}
+
+constexpr float kSweepH = 60.0f / 32;  // H of the field sweeps
+
+void anisotropy(const std::string& out) {
+  const auto T = InterpolationScheme::TSC;
+  const auto F2 = FiniteDiffScheme::TWO_POINT;
+  const auto L = GreensFunction::DISCRETE_LAPLACIAN;
+  fieldSweep(out, "positions.dat", "field.dat", v3(30, 30, 15), v3(1, 0, 0), T, F2, L, 0);
+  fieldSweep(out, "positions_offset.dat", "field_offset.dat", v3(30 - kSweepH / 2, 30, 15), v3(1, 0, 0), T,
+             F2, L, 0);
+  const float s = 1 / std::sqrt(2.0f);
+  fieldSweep(out, "positions_diag.dat", "field_diag.dat", v3(30, 30, 15), v3(s, s, 0), T, F2, L, 0);
+}
+
+void finiteDiffRelError(const std::string& out) {
+  const auto T = InterpolationScheme::TSC;
+  const auto L = GreensFunction::DISCRETE_LAPLACIAN;
+  fieldSweep(out, "positions-2.dat", "field-2.dat", v3(30, 30, 15), v3(1, 0, 0), T,
+             FiniteDiffScheme::TWO_POINT, L, 0);
+  fieldSweep(out, "positions-4.dat", "field-4.dat", v3(30, 30, 15), v3(1, 0, 0), T,
+             FiniteDiffScheme::FOUR_POINT, L, 0);
+}
+
+void assignmentSchemes(const std::string& out) {
+  const auto F4 = FiniteDiffScheme::FOUR_POINT;
+  const auto L = GreensFunction::DISCRETE_LAPLACIAN;
+  fieldSweep(out, "positions-tsc.dat", "field-tsc.dat", v3(30, 30, 15), v3(1, 0, 0),
+             InterpolationScheme::TSC, F4, L, 0);
+  fieldSweep(out, "positions-cic.dat", "field-cic.dat", v3(30, 30, 15), v3(1, 0, 0),
+             InterpolationScheme::CIC, F4, L, 0);
+  fieldSweep(out, "positions-ngp.dat", "field-ngp.dat", v3(30, 30, 15), v3(1, 0, 0),
+             InterpolationScheme::NGP, F4, L, 0);
+}
+
+void poorLaplace(const std::string& out) {
+  const auto T = InterpolationScheme::TSC;
+  const auto F4 = FiniteDiffScheme::FOUR_POINT;
+  fieldSweep(out, "positions-poor-man.dat", "field-poor-man.dat", v3(30, 30, 15), v3(1, 0, 0), T, F4,
+             GreensFunction::POOR_MAN, 0);
+  fieldSweep(out, "positions-discrete-lap.dat", "field-discrete-lap.dat", v3(30, 30, 15), v3(1, 0, 0), T,
+             F4, GreensFunction::DISCRETE_LAPLACIAN, 0);
+}
+
+void pmOptimal(const std::string& out) {
+  const auto T = InterpolationScheme::TSC;
+  const auto F4 = FiniteDiffScheme::FOUR_POINT;
+  fieldSweep(out, "positions-s1.dat", "field-s1.dat", v3(30, 30, 15), v3(1, 0, 0), T, F4,
+             GreensFunction::S1_OPTIMAL, 4 * kSweepH);
+  fieldSweep(out, "positions-s2.dat", "field-s2.dat", v3(30, 30, 15), v3(1, 0, 0), T, F4,
+             GreensFunction::S2_OPTIMAL, 4 * kSweepH);
+}
+
+void pmOptimalVaryingDiameter(const std::string& out) {
+  const auto T = InterpolationScheme::TSC;
+  const auto F4 = FiniteDiffScheme::FOUR_POINT;
+  for (const auto gf : {GreensFunction::S1_OPTIMAL, GreensFunction::S2_OPTIMAL}) {
+    const std::string tag = gf == GreensFunction::S1_OPTIMAL ? "s1" : "s2";
+    for (int i = 5; i <= 30; ++i) {
+      const std::string positions = "positions-" + tag + ".dat";
+      const std::string field = "field-" + tag + "-" + std::to_string(i) + ".dat";
+      fieldSweep(out, positions.c_str(), field.c_str(), v3(30, 30, 15), v3(1, 0, 0), T, F4, gf,
+                 0.2f * i * kSweepH);
+    }
+  }
+}
+
+void pmOptimalAssignments(const std::string& out) {
+  const std::pair<InterpolationScheme, const char*> schemes[] = {
+      {InterpolationScheme::NGP, "NGP"}, {InterpolationScheme::CIC, "CIC"}, {InterpolationScheme::TSC, "TSC"}};
+  for (const auto& [is, name] : schemes) {
+    const std::string field = std::string("field-s1-") + name + ".dat";
+    fieldSweep(out, "positions-s1.dat", field.c_str(), v3(30, 30, 15), v3(1, 0, 0), is,
+               FiniteDiffScheme::FOUR_POINT, GreensFunction::S1_OPTIMAL, 4 * kSweepH);
+  }
+}
+
 }  // namespace
 
 int main(int argc, char* argv[]) {
@@ -167,6 +277,13 @@ int main(int argc, char* argv[]) {
         {"galaxy-collision-sim-p3m", [&] { galaxyCollision(out, true); }},
         {"cluster-sim-pm", [&] { plummer(out, false); }},
         {"cluster-sim-p3m", [&] { plummer(out, true); }},
+        {"anisotropy", [&] { anisotropy(out); }},
+        {"finite-diff-err", [&] { finiteDiffRelError(out); }},
+        {"assignment-schemes", [&] { assignmentSchemes(out); }},
+        {"poor-man-vs-laplacian", [&] { poorLaplace(out); }},
+        {"pm-optimal", [&] { pmOptimal(out); }},
+        {"pm-optimal-var-diameter", [&] { pmOptimalVaryingDiameter(out); }},
+        {"pm-optimal-assignments", [&] { pmOptimalAssignments(out); }},
         // galaxySimulationPMTiming / P3MTiming (source/demos.cpp:779-836, 953-1016): "n seconds"
         {"galaxy-sim-pm-timing",
          [&] {

@@ -2,7 +2,7 @@
 compiled from the reference sources by oracle/Makefile).
 
 Run where the reference sources exist:
-    python tests/golden/make_golden.py [diagnostics|recorder|samplers]
+    python tests/golden/make_golden.py [diagnostics|recorder|samplers|field_sweeps]
 (with an argument, only that fixture is rewritten).
 Every case is a small seeded input; each fixture stores the inputs, the settings and the
 reference's outputs (float32), so tests on a machine without the reference still compare
@@ -117,6 +117,36 @@ def recorder_fixture():
                          **_cfg_arrays(c),
                          **{f"file:{k}": np.frombuffer(b, np.uint8) for k, b in files.items()})
     np.savez_compressed(os.path.join(HERE, "recorder.npz"),
+                        **{f"{c}/{k}": a for c, dd in out.items() for k, a in dd.items()})
+
+
+def field_sweeps_fixture():
+    """The reference's positions.dat / field.dat of three PM field sweeps of its demos
+    (source/demos.cpp:109-591): a mass-1 particle with 399 massless tracers every 0.075 along x
+    from (30, 30, 15), 64 x 64 x 32 mesh, box 60 x 60 x 30, H = 60/32, G = 4.5e-3, DT = 1, one
+    iteration with the field recorded (the scenario command line's anisotropy,
+    pm-optimal and assignment-schemes options write the same runs)."""
+    import tempfile
+    n = 400
+    pos = np.zeros((n, 3), np.float32)
+    for i in range(n):  # linearSpacing: center + i * dx * dir, in float
+        pos[i] = np.float32(30) + np.float32(i) * np.float32(0.075), 30, 15
+    vel = np.zeros((n, 3), np.float32)
+    mass = np.zeros(n, np.float32)
+    mass[0] = 1
+    H = np.float32(60.0) / np.float32(32)
+    out = {}
+    for name, interp, fds, greens, diam in (("aniso", 2, 0, 0, 0.0), ("optimal_s2", 2, 1, 2, 4 * H),
+                                              ("ngp", 0, 1, 0, 0.0)):
+        cfg = O.PMConfig(grid=(64, 64, 32), box=(60.0, 60.0, 30.0), H=float(H), DT=1.0, G=4.5e-3,
+                         interpolation=interp, finite_diff=fds, greens=greens, diameter=float(diam))
+        with tempfile.TemporaryDirectory() as d:
+            esc, files = O.ref_run_files(cfg, None, pos, vel, mass, 1, d, diagnostics=False,
+                                         record_field=True)
+        assert not esc
+        out[name] = {"positions": np.frombuffer(files["positions.dat"], np.uint8),
+                     "field": np.frombuffer(files["field.dat"], np.uint8)}
+    np.savez_compressed(os.path.join(HERE, "field_sweeps.npz"),
                         **{f"{c}/{k}": a for c, dd in out.items() for k, a in dd.items()})
 
 
@@ -248,8 +278,11 @@ if __name__ == "__main__":
         recorder_fixture()
     elif sys.argv[1:] == ["samplers"]:
         samplers_fixture()
+    elif sys.argv[1:] == ["field_sweeps"]:
+        field_sweeps_fixture()
     else:
         main()
         diagnostics_fixture()
         recorder_fixture()
         samplers_fixture()
+        field_sweeps_fixture()
