@@ -127,3 +127,35 @@ def test_p3m_full_size_disk(gpu_lib):
     assert rel_rms(acc[idx], f64) < 1e-5
     p3m.close()
     pm.close()
+
+
+def test_p3m_dense_cluster_heavy_units(gpu_lib):
+    """A cluster dense enough that some units of the table pass are heavy (taken by whole CTAs,
+    their candidate chunks split over the CTA's warps) or medium: forces on a subsample vs the
+    FP64 oracle, and two evaluations bit-identical (the warps' partial sums are added in a fixed
+    order)."""
+    rng = np.random.default_rng(11)
+    H = 30.0 / 32
+    n = 40000
+    pos = np.concatenate([rng.normal(15.0, 0.6, (n // 2, 3)), rng.normal(15.0, 2.5, (n // 4, 3)),
+                          rng.uniform(4.0, 26.0, (n - n // 2 - n // 4, 3))])
+    pos = np.clip(pos, 4.0, 26.0).astype(np.float32)
+    vel = rng.normal(0, 0.01, (n, 3)).astype(np.float32)
+    mass = np.full(n, 1.0 / n, np.float32)
+    cfg = O.PMConfig(grid=(32, 32, 32), box=(30.0, 30.0, 30.0), H=H, DT=0.05, G=1.0,
+                     interpolation=2, finite_diff=0, greens=2, diameter=3 * H)
+    q = O.P3MConfig(comp_box=(30.0, 30.0, 30.0), cutoff=3 * H, diameter=3 * H, softening=0.0,
+                    cloud_shape=1)
+    pm, p3m = make_p3m(cfg, q, pos, vel, mass)
+    p3m.force()
+    acc1 = pm.getParticles()[2].copy()
+    order, counts, dims = p3m.getCellLists()
+    assert counts.max() >= 1024  # units against this cell cost at least the heavy minimum
+    p3m.force()
+    acc2 = pm.getParticles()[2]
+    np.testing.assert_array_equal(acc1, acc2)
+    idx = np.sort(rng.choice(n, 1200, replace=False)).astype(np.int32)
+    f64 = O.port_p3m_accel_targets(cfg, q, pos, vel, mass, idx, prec=1)
+    assert rel_rms(acc1[idx], f64) < 1e-5
+    p3m.close()
+    pm.close()
