@@ -9,10 +9,14 @@
 // A CTA takes a chunk of consecutive (spatially sorted) particles, reduces the bounding box of
 // their stencils and, when it fits, accumulates into a shared-memory tile that is flushed with
 // one global atomic per touched cell; chunks whose box is too large (sparse or unsorted
-// regions) add straight into global memory.  The tile holds 4,096 cells (32 KB; a 64 KB tile,
-// which would also take the 17^3-cell chunks of uniform regions, measured slower: fewer
-// resident CTAs) and is flushed a mesh row per warp.  Mesh indices wrap periodically (the
-// reference leaves them unwrapped, undefined beyond the mesh edge).
+// regions) add straight into global memory.  The tile holds 4,096 cells (32 KB as two 32-bit
+// planes, see tile_add; a 64 KB tile, which would also take the 17^3-cell chunks of uniform
+// regions, measured slower: fewer resident CTAs) and is flushed a mesh row per warp.  Where a
+// chunk holds few particles per tile cell the direct path is the cheaper one: chunks cut at
+// aligned 16 x 16 x 8-cell blocks, whose boxes all fit, measured slower with every chunk on
+// the tile and no faster with the tile kept for chunks of at most 8 cells per particle.  Mesh
+// indices wrap periodically (the reference leaves them unwrapped, undefined beyond the mesh
+// edge).
 #include "deposit_body.cuh"
 
 namespace pmgb {
@@ -26,7 +30,7 @@ __global__ void __launch_bounds__(DEP_THREADS) deposit_kernel(const float4* __re
                                                               const int* __restrict__ stop) {
   if (stop && *stop) return;
   extern __shared__ u64 dep_tile[];
-  __shared__ int red[DEP_THREADS / 32];
+  __shared__ int red[DEP_RED_WORDS];
   deposit_block<IS, DEP_PPT, DEP_TILE_PM>(pm, blockIdx.x * DEP_CHUNK, n, m, scale, rho, dep_tile, red);
 }
 

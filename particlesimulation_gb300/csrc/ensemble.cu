@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(DEP_THREADS) ens_deposit_kernel(const EnsSys* 
                                                                   u64* __restrict__ rho,
                                                                   int* __restrict__ flags) {
   __shared__ u64 tile[DEP_TILE];
-  __shared__ int red[DEP_THREADS / 32];
+  __shared__ int red[DEP_RED_WORDS];
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const int2 w = items[it];
     if (ens_stopped(flags, w.x)) {
