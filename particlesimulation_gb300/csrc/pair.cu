@@ -220,13 +220,15 @@ __global__ void __launch_bounds__(PAIR_THREADS) pair_kernel(
 //  * the table is kept in intercept form per segment, f(xi) = A[t] + xi S[t] with
 //    S[t] = T[t+1] - T[t] (float, as the reference forms it) and A[t] = T[t] - t S[t] (double,
 //    rounded once): one FMA instead of forming xi - t;
-//  * positions enter in units of the table spacing delta, relative to the slice's first
-//    particle (so differences keep code-unit precision): |r|^2 is xi, and 1/delta is folded into
-//    the table;
-//  * t = floor(xi) is one round-down add of 1.5 * 2^23 (FADD.RM), whose bits give the lane's
-//    table entry by one 32-bit multiply-add into a shared-memory address;
-//  * the cutoff test is folded into the table: segments t >= 499 (xi >= 499, i.e.
-//    r^2 >= re^2) are zero, and xi is clamped to 499.5 so t never leaves the table;
+//  * positions enter in units of sqrt(512) table spacings delta, relative to the slice's first
+//    particle (so differences keep code-unit precision): |r|^2 is xs = xi / 512, and the last
+//    multiply-add of |r|^2 saturates it to [0, 1] (fma.sat, no extra instruction), which is the
+//    bound check of the lookup; 512 is folded into S and 1/delta into the table;
+//  * t = floor(512 xs) is one round-down multiply-add of xs by 512 plus 1.5 * 2^23 (FFMA.RM,
+//    exact: 512 xs is a power-of-two scaling), whose bits give the lane's table entry by one
+//    32-bit multiply-add into a shared-memory address;
+//  * the cutoff test is folded into the table: segments 499 <= t <= 512 (xi >= 499, i.e.
+//    r^2 >= re^2) are zero;
 //  * with equal masses (every benchmark workload) the mass is folded into the table;
 //  * the table is replicated 16 times, copy (lane mod 16) for each lane, so the per-lane lookups
 //    of a half warp fall into 16 distinct bank pairs whatever their segments (an 8-byte load
@@ -236,7 +238,7 @@ __global__ void __launch_bounds__(PAIR_THREADS) pair_kernel(
 // search (32 probes per round).  Per-chunk partial sums are added with Kahan compensation.
 constexpr int SLOT_IPL = 2;                  // i particles per lane
 constexpr int SLOT_SLICE = 32 * SLOT_IPL;    // particles per work item
-constexpr int SLOT_TAB = 500;                // segments 0..499 (499 = zero)
+constexpr int SLOT_TAB = 513;                // segments 0..512 (499..512 = zero)
 constexpr int SLOT_REP = 16;                 // table copies (lane mod 16)
 constexpr int NNB = 27;                      // neighbour cells (and slots) per particle
 constexpr int SLOT_THREADS = 512;
@@ -257,16 +259,18 @@ struct SlotI {
 // tab_base: shared-memory address of this lane's table copy minus bits(kMagic) * SLOT_REP * 8,
 // so that segment t = bits(kMagic + t) - bits(kMagic) is at bits(kMagic + t) * SLOT_REP * 8 +
 // tab_base (32-bit arithmetic modulo 2^32): one multiply-add per lookup.
-// Positions are in units of the table spacing delta (relative to the slice's first particle), so
-// |r|^2 is xi itself; the table holds f / delta for the unscaled difference vector.
+// Positions are in units of sqrt(512) delta (relative to the slice's first particle), so |r|^2
+// is xs = xi / 512, saturated to [0, 1]; the table holds f / (sqrt(512) delta) for the scaled
+// difference vector, with the slopes times 512.
 template <bool EQM>
 __device__ __forceinline__ void slot_pair(SlotI& I, const float4& q, u32 tab_base) {
   const float dx = I.p.x - q.x, dy = I.p.y - q.y, dz = I.p.z - q.z;
-  const float xi = fminf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)), 499.5f);
-  const u32 bits = __float_as_uint(__fadd_rd(xi, kMagic));  // kMagic + floor(xi)
+  float xs;
+  asm("fma.rn.sat.f32 %0, %1, %1, %2;" : "=f"(xs) : "f"(dz), "f"(fmaf(dy, dy, dx * dx)));
+  const u32 bits = __float_as_uint(__fmaf_rd(xs, 512.0f, kMagic));  // kMagic + floor(512 xs)
   float2 ab;
   asm("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(ab.x), "=f"(ab.y) : "r"(bits * (SLOT_REP * 8) + tab_base));
-  float f = fmaf(xi, ab.y, ab.x);
+  float f = fmaf(xs, ab.y, ab.x);
   if (!EQM) f *= q.w;
   I.px = fmaf(f, dx, I.px);
   I.py = fmaf(f, dy, I.py);
@@ -472,8 +476,8 @@ __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
   float4 (*jbuf)[32] = reinterpret_cast<float4 (*)[32]>(slot_smem);
   float4* part = slot_smem + SLOT_WARPS * 32;
   float2* tab_all = reinterpret_cast<float2*>(part + SLOT_WARPS * SLOT_SLICE);
-  // coordinates are scaled by sc = 1/delta (sc^2 = 1/delta^2 to float rounding)
-  const float sc = (float)sqrt((double)pp.inv_d2);
+  // coordinates are scaled by sc = 1/(sqrt(512) delta) (512 sc^2 = 1/delta^2 to float rounding)
+  const float sc = (float)sqrt((double)pp.inv_d2 / 512.0);
   {
     // every particle has the same mass when EQM: fold it into the table, with 1/sc
     const double mj = (EQM ? (double)__ldg(&pm[0].w) : 1.0) / (double)sc;
@@ -483,7 +487,7 @@ __global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
         const float a = table[t];
         const float s = table[t + 1] - a;
         const double A = (double)a - (double)t * (double)s;
-        ab = make_float2((float)(A * mj), (float)((double)s * mj));
+        ab = make_float2((float)(A * mj), (float)((double)s * 512.0 * mj));
       }
 #pragma unroll
       for (int c = 0; c < SLOT_REP; ++c) tab_all[t * SLOT_REP + c] = ab;
