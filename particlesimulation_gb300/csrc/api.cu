@@ -208,11 +208,31 @@ int after_drift(pmgb_pm* h, int tag) {
   return rec_after_drift(h, tag);
 }
 
-int run_loop(pmgb_pm* h, int sim_length, int* steps_done) {
-  PMGB_CUDA_TRY(cudaMemsetAsync(h->flags, 0, sizeof(int), h->st));
+// Run start: the stop and timeout words cleared, the escape iteration at INT_MAX.
+int clear_run_flags(pmgb_pm* h) {
+  PMGB_CUDA_TRY(cudaMemsetAsync(h->flags, 0, 3 * sizeof(int), h->st));
   const int big = 0x7FFFFFFF;
   PMGB_CUDA_TRY(cudaMemcpyAsync(h->flags + 1, &big, sizeof(int), cudaMemcpyHostToDevice, h->st));
-  int rc = diag_run_begin(h);
+  return PMGB_OK;
+}
+
+// Run end (after the stream synchronised): flags[0..2] read back; a bounded wait that gave up
+// comes first, then an escape.
+int run_status(const int flags[3], int* steps_done, int done_steps) {
+  if (flags[kFlagTimeout]) return set_error("a bounded device wait gave up"), PMGB_ETIMEOUT;
+  if (flags[0]) {
+    if (steps_done) *steps_done = flags[1];
+    set_error("Particle moved outside the computational box.");
+    return PMGB_EESCAPED;
+  }
+  if (steps_done) *steps_done = done_steps;
+  return PMGB_OK;
+}
+
+int run_loop(pmgb_pm* h, int sim_length, int* steps_done) {
+  int rc = clear_run_flags(h);
+  if (rc) return rc;
+  rc = diag_run_begin(h);
   if (rc) return rc;
   // initial force, half kick (setHalfStepVelocities) and the drift of iteration 0
   rc = force(h, 1, 0.5f, 1, 0, false);
@@ -224,16 +244,10 @@ int run_loop(pmgb_pm* h, int sim_length, int* steps_done) {
     if (rc) return rc;
     if (t < sim_length && (rc = after_drift(h, t + 1))) return rc;
   }
-  int flags[2];
-  PMGB_CUDA_TRY(cudaMemcpyAsync(flags, h->flags, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  int flags[3];
+  PMGB_CUDA_TRY(cudaMemcpyAsync(flags, h->flags, 3 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
   PMGB_CUDA_TRY(cudaStreamSynchronize(h->st));
-  if (flags[0]) {
-    if (steps_done) *steps_done = flags[1];
-    set_error("Particle moved outside the computational box.");
-    return PMGB_EESCAPED;
-  }
-  if (steps_done) *steps_done = sim_length + 1;
-  return PMGB_OK;
+  return run_status(flags, steps_done, sim_length + 1);
 }
 
 }  // namespace
@@ -402,10 +416,15 @@ int pmgb_pm_init_greens_function(pmgb_pm* h) {
 int pmgb_pm_method_step(pmgb_pm* h) {
   if (!h) return set_error("null handle"), PMGB_EINVAL;
   PMGB_CUDA_TRY(cudaMemsetAsync(h->flags, 0, sizeof(int), h->st));
+  PMGB_CUDA_TRY(cudaMemsetAsync(h->flags + kFlagTimeout, 0, sizeof(int), h->st));
   int rc = force(h, 0, 0.f, 0, 0, true);
   if (rc) return rc;
+  int timed_out = 0;
+  if (h->closure)  // the closure's tensor-core kernel is the one with bounded waits
+    PMGB_CUDA_TRY(cudaMemcpyAsync(&timed_out, h->flags + kFlagTimeout, sizeof(int), cudaMemcpyDeviceToHost, h->st));
   PMGB_CUDA_TRY(cudaStreamSynchronize(h->st));
   for (int s = 0; s < 5; ++s) cudaEventElapsedTime(&h->stage_ms[s], h->ev[s], h->ev[s + 1]);
+  if (timed_out) return set_error("a bounded device wait gave up"), PMGB_ETIMEOUT;
   return PMGB_OK;
 }
 
@@ -413,9 +432,8 @@ int pmgb_pm_advance(pmgb_pm* h, int n_steps, int* steps_done, float* device_ms) 
   if (!h) return set_error("null handle"), PMGB_EINVAL;
   if (n_steps < 0) return set_error("negative step count"), PMGB_EINVAL;
   PMGB_CUDA_TRY(cudaStreamSynchronize(h->st));
-  PMGB_CUDA_TRY(cudaMemsetAsync(h->flags, 0, sizeof(int), h->st));
-  const int big = 0x7FFFFFFF;
-  PMGB_CUDA_TRY(cudaMemcpyAsync(h->flags + 1, &big, sizeof(int), cudaMemcpyHostToDevice, h->st));
+  int rc0 = clear_run_flags(h);
+  if (rc0) return rc0;
   PMGB_CUDA_TRY(cudaEventRecord(h->ev[0], h->st));
   if (n_steps > 0) {
     // the first drift of the loop body, then (force, kick, drift) with the last drift left out
@@ -433,17 +451,11 @@ int pmgb_pm_advance(pmgb_pm* h, int n_steps, int* steps_done, float* device_ms) 
     }
   }
   PMGB_CUDA_TRY(cudaEventRecord(h->ev[5], h->st));
-  int flags[2];
-  PMGB_CUDA_TRY(cudaMemcpyAsync(flags, h->flags, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  int flags[3];
+  PMGB_CUDA_TRY(cudaMemcpyAsync(flags, h->flags, 3 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
   PMGB_CUDA_TRY(cudaStreamSynchronize(h->st));
   if (device_ms) cudaEventElapsedTime(device_ms, h->ev[0], h->ev[5]);
-  if (flags[0]) {
-    if (steps_done) *steps_done = flags[1];
-    set_error("Particle moved outside the computational box.");
-    return PMGB_EESCAPED;
-  }
-  if (steps_done) *steps_done = n_steps;
-  return PMGB_OK;
+  return run_status(flags, steps_done, n_steps);
 }
 
 int pmgb_pm_run_recorded(pmgb_pm* h, pmgb_recorder* rec, int sim_length, int collect_diagnostics,

@@ -10,8 +10,10 @@
 //                 by the patch mass S, and the particle's offset from the patch centre in cell
 //                 units (3)
 //   network       67 -> 64 -> 64 -> 64 -> 3, GELU, BF16 weights and activations, FP32
-//                 accumulation (mma.sync m16n8k16 bf16 tensor-core tiles, one warp per 16
-//                 particles; layer outputs stay in registers as the next layer's operands)
+//                 accumulation.  Inference: tcgen05.mma from shared memory into TMEM, 128
+//                 particles per CTA (the tcgen05 forward below).  Training (forward, backward):
+//                 mma.sync m16n8k16 tiles, one warp per 16 rows, layer outputs kept in
+//                 registers as the next layer's operands
 //   output  (3)   residual / (S * c), c = 1 / (4 pi HC'^2)  (the residual is linear in the
 //                 masses, so scaling by S makes the map scale free)
 // Training pairs are the exact residual from the plain P3M itself (full-cutoff force minus
@@ -246,64 +248,267 @@ __device__ __forceinline__ float features(const ReducedMesh& rm, const float* __
   return S;
 }
 
+// ------------------------------------------------------------------ tcgen05 forward --
+// Inference runs on the 5th-generation tensor cores: a CTA of 128 threads takes tiles of 128
+// particles (thread r = row r = TMEM lane r = the accumulator row of an M = 128 MMA).  Per
+// layer one thread issues tcgen05.mma.kind::f16 (BF16 operands from shared memory, FP32
+// accumulator in 64 TMEM columns) over the K slices of 16 and commits to an mbarrier; every
+// thread then reads its row from TMEM (tcgen05.ld 32x32b), adds the bias, applies GELU and
+// writes the BF16 activations back to shared memory as the next layer's A operand.  The output
+// layer is padded to N = 16 (M = 128 takes N in multiples of 16).  Operands are in the
+// no-swizzle K-major layout: 8-row x 16-byte core matrices, the core matrix of row group g and
+// K group j at j * kstride + g * 128 bytes; the matrix descriptor's leading byte offset is the
+// K-group stride, the stride byte offset the row-group stride.  Every wait on the mbarrier is
+// bounded; a wait that gives up sets err[0] and the kernel runs on to its end (uniform control
+// flow), and the host reports PMGB_ETIMEOUT.  Training keeps the mma.sync kernels above.
+constexpr int TC_ROWS = 128;
+constexpr int TC_THREADS = 128;
+constexpr int TC_N4 = 16;                   // output layer, padded
+constexpr int TC_COLS = 64;                 // TMEM columns (power of two >= 32)
+constexpr u32 TC_KX = TC_ROWS * 16;         // K-group stride of the 128-row A operands (bytes)
+constexpr u32 TC_KW = CL_H * 16;            // K-group stride of the 64-row weight operands
+constexpr u32 TC_KW4 = TC_N4 * 16;          // K-group stride of the output layer's weights
+constexpr int TC_WAIT_SPINS = 1 << 24;      // bound of an mbarrier wait (far beyond a layer's MMAs)
+
+struct TcSmem {
+  alignas(16) bf16 w1[CL_H * CL_K0];
+  alignas(16) bf16 w2[CL_H * CL_H];
+  alignas(16) bf16 w3[CL_H * CL_H];
+  alignas(16) bf16 w4[TC_N4 * CL_H];
+  alignas(16) bf16 x[TC_ROWS * CL_K0];     // layer-1 inputs
+  alignas(16) bf16 h[TC_ROWS * CL_H];      // hidden activations (one layer at a time)
+  float bias[3 * CL_H + TC_N4];
+  float spatch[TC_ROWS];
+  u64 mbar;
+  u32 tmem;
+};
+
+__device__ __forceinline__ u32 smem_addr(const void* p) { return (u32)__cvta_generic_to_shared(p); }
+
+// byte offset of element (r, k) in the canonical layout with K-group stride kstride
+__device__ __forceinline__ u32 canon(int r, int k, u32 kstride) {
+  return (u32)(k >> 3) * kstride + (u32)(r >> 3) * 128u + (u32)(r & 7) * 16u + (u32)(k & 7) * 2u;
+}
+
+// shared-memory matrix descriptor: start, leading byte offset (K-group stride), stride byte
+// offset (row-group stride, 128), the fixed 0b001 at bits 46-48, no swizzle
+__device__ __forceinline__ u64 tc_desc(u32 saddr, u32 kstride) {
+  return (u64)((saddr >> 4) & 0x3FFFu) | ((u64)((kstride >> 4) & 0x3FFFu) << 16) |
+         ((u64)(128u >> 4) << 32) | (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, M x N
+__host__ __device__ constexpr u32 tc_idesc(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((u32)(N >> 3) << 17) | ((u32)(M >> 4) << 24);
+}
+
+// D (TMEM) = A x B^T over nks K slices of 16, then a commit to the mbarrier (one thread)
+__device__ __forceinline__ void tc_mma_layer(u32 tmem, u32 a, u32 akstride, u32 b, u32 bkstride,
+                                             int nks, u32 idesc, u32 mbar) {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  for (int ks = 0; ks < nks; ++ks) {
+    const u64 ad = tc_desc(a + 2u * ks * akstride, akstride);
+    const u64 bd = tc_desc(b + 2u * ks * bkstride, bkstride);
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+        :: "r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(ks > 0 ? 1u : 0u) : "memory");
+  }
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+               :: "r"(mbar) : "memory");
+}
+
+// bounded wait for the mbarrier phase of the given parity; false if it gave up
+__device__ __forceinline__ bool tc_wait(u32 mbar, u32 parity) {
+  u32 done = 0;
+  for (int it = 0; it < TC_WAIT_SPINS && !done; ++it) {
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done) : "r"(mbar), "r"(parity) : "memory");
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  return done != 0;
+}
+
+// this thread's TMEM lane (its warp's 32-lane block), columns 0..63 / 0..15
+__device__ __forceinline__ void tc_ld64(u32 taddr, float (&v)[64]) {
+  u32 r[64];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x64.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,"
+      "%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,"
+      "%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
+        "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
+        "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
+        "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]),
+        "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 64; ++j) v[j] = __uint_as_float(r[j]);
+}
+__device__ __forceinline__ void tc_ld16(u32 taddr, float (&v)[16]) {
+  u32 r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// row r of a canonical operand from 8 K groups of 8 values (16-byte stores)
+template <int KG>
+__device__ __forceinline__ void tc_store_row(unsigned char* base, int r, u32 kstride, const float* v) {
+#pragma unroll
+  for (int j = 0; j < KG; ++j) {
+    uint4 q;
+    q.x = pack_bf16(v[8 * j + 0], v[8 * j + 1]);
+    q.y = pack_bf16(v[8 * j + 2], v[8 * j + 3]);
+    q.z = pack_bf16(v[8 * j + 4], v[8 * j + 5]);
+    q.w = pack_bf16(v[8 * j + 6], v[8 * j + 7]);
+    *reinterpret_cast<uint4*>(base + canon(r, 8 * j, kstride)) = q;
+  }
+}
+
+// Prologue of a CTA: weights (from the BF16 image) and biases into shared memory, the
+// mbarrier, 64 TMEM columns (warp 0).  Ends with a barrier.
+__device__ void tc_setup(TcSmem& s, const bf16* __restrict__ img, const float* __restrict__ p) {
+  unsigned char* w1 = reinterpret_cast<unsigned char*>(s.w1);
+  unsigned char* w2 = reinterpret_cast<unsigned char*>(s.w2);
+  unsigned char* w3 = reinterpret_cast<unsigned char*>(s.w3);
+  unsigned char* w4 = reinterpret_cast<unsigned char*>(s.w4);
+  for (int e = threadIdx.x; e < CL_H * CL_K0; e += blockDim.x) {
+    const int n = e / CL_K0, k = e % CL_K0;
+    *reinterpret_cast<bf16*>(w1 + canon(n, k, TC_KW)) = img[IMG_W1 + n * S80 + k];
+  }
+  for (int e = threadIdx.x; e < CL_H * CL_H; e += blockDim.x) {
+    const int n = e / CL_H, k = e % CL_H;
+    *reinterpret_cast<bf16*>(w2 + canon(n, k, TC_KW)) = img[IMG_W2 + n * S64 + k];
+    *reinterpret_cast<bf16*>(w3 + canon(n, k, TC_KW)) = img[IMG_W3 + n * S64 + k];
+  }
+  for (int e = threadIdx.x; e < TC_N4 * CL_H; e += blockDim.x) {
+    const int n = e / CL_H, k = e % CL_H;
+    *reinterpret_cast<bf16*>(w4 + canon(n, k, TC_KW4)) =
+        n < CL_NO ? img[IMG_W4 + n * S64 + k] : __float2bfloat16_rn(0.f);
+  }
+  for (int i = threadIdx.x; i < CL_H; i += blockDim.x) {
+    s.bias[i] = p[OFF_B1 + i];
+    s.bias[CL_H + i] = p[OFF_B2 + i];
+    s.bias[2 * CL_H + i] = p[OFF_B3 + i];
+  }
+  for (int i = threadIdx.x; i < TC_N4; i += blockDim.x) s.bias[3 * CL_H + i] = i < CL_NO ? p[OFF_B4 + i] : 0.f;
+  if (threadIdx.x == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(&s.mbar)) : "memory");
+  if (threadIdx.x < 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 :: "r"(smem_addr(&s.tmem)), "r"(TC_COLS) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// Forward pass of one tile whose inputs are in s.x: returns this thread's row of the output
+// layer (3 values).  phase: the mbarrier parity of the next commit (advanced by 4).
+__device__ __forceinline__ void tc_forward(TcSmem& s, u32& phase, int* __restrict__ err, float y[3]) {
+  const u32 tmem = s.tmem;
+  const u32 taddr = tmem + ((u32)(threadIdx.x & ~31) << 16);
+  const u32 mbar = smem_addr(&s.mbar);
+  const u32 xa = smem_addr(s.x), ha = smem_addr(s.h);
+  const u32 wa[3] = {smem_addr(s.w1), smem_addr(s.w2), smem_addr(s.w3)};
+  unsigned char* hb = reinterpret_cast<unsigned char*>(s.h);
+  // inputs written by every thread: make them visible to the tensor cores
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+#pragma unroll 1
+  for (int l = 0; l < 3; ++l) {
+    if (threadIdx.x == 0)
+      tc_mma_layer(tmem, l == 0 ? xa : ha, TC_KX, wa[l], TC_KW, l == 0 ? CL_K0 / 16 : CL_H / 16,
+                   tc_idesc(TC_ROWS, CL_H), mbar);
+    if (!tc_wait(mbar, phase & 1u)) atomicExch(err, 1);
+    ++phase;
+    float z[64];
+    tc_ld64(taddr, z);
+    const float* b = s.bias + l * CL_H;
+#pragma unroll
+    for (int j = 0; j < 64; ++j) z[j] = gelu(z[j] + b[j]);
+    tc_store_row<CL_H / 8>(hb, threadIdx.x, TC_KX, z);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    tc_mma_layer(tmem, ha, TC_KX, smem_addr(s.w4), TC_KW4, CL_H / 16, tc_idesc(TC_ROWS, TC_N4), mbar);
+  if (!tc_wait(mbar, phase & 1u)) atomicExch(err, 1);
+  ++phase;
+  float o[16];
+  tc_ld16(taddr, o);
+  const float* b4 = s.bias + 3 * CL_H;
+  y[0] = o[0] + b4[0];
+  y[1] = o[1] + b4[1];
+  y[2] = o[2] + b4[2];
+  // the next tile rewrites s.x and TMEM only after every thread is past its loads
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+}
+
+__device__ __forceinline__ void tc_teardown(TcSmem& s) {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (threadIdx.x < 32)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(s.tmem), "r"(TC_COLS) : "memory");
+}
+
 // ------------------------------------------------------------------ inference --------
 // acc[i] += MLP(features(i)) * S * c, for the particles of this handle (sorted order).
-__global__ void __launch_bounds__(CL_THREADS) closure_infer_kernel(
+__global__ void __launch_bounds__(TC_THREADS) closure_infer_kernel(
     const float4* __restrict__ pm, int n, ReducedMesh rm, const float* __restrict__ occ,
     const bf16* __restrict__ img, const float* __restrict__ params, float4* __restrict__ acc,
-    const int* __restrict__ stop) {
+    const int* __restrict__ stop, int* __restrict__ err) {
   if (*stop) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemMLP& s = *reinterpret_cast<SmemMLP*>(smem_raw);
-  bf16* xs_all = reinterpret_cast<bf16*>(smem_raw + sizeof(SmemMLP));
-  float* sp_all = reinterpret_cast<float*>(smem_raw + sizeof(SmemMLP) + CL_WARPS * 16 * S80 * sizeof(bf16));
-  load_mlp_smem(s, img, params);
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  bf16* xs = xs_all + warp * 16 * S80;
-  float* spatch = sp_all + warp * 16;
-  const int tiles = (n + 15) / 16;
-  for (int tile = blockIdx.x * CL_WARPS + warp; tile < tiles; tile += gridDim.x * CL_WARPS) {
-    const int r0 = tile * 16;
-    // features: lane r < 16 builds row r
-    if (lane < 16) {
-      const int i = r0 + lane;
-      float f[CL_K0];
-      float S = 0.f;
-      if (i < n) {
-        const float4 p = pm[i];
-        S = features(rm, occ, p.x, p.y, p.z, f);
-      } else {
+  TcSmem& s = *reinterpret_cast<TcSmem*>(smem_raw);
+  tc_setup(s, img, params);
+  unsigned char* xb = reinterpret_cast<unsigned char*>(s.x);
+  u32 phase = 0;
+  const int tiles = (n + TC_ROWS - 1) / TC_ROWS;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const int i = tile * TC_ROWS + threadIdx.x;
+    float f[CL_K0];
+    float S = 0.f;
+    if (i < n) {
+      const float4 p = pm[i];
+      S = features(rm, occ, p.x, p.y, p.z, f);
+    } else {
 #pragma unroll
-        for (int k = 0; k < CL_K0; ++k) f[k] = 0.f;
-      }
-#pragma unroll
-      for (int c = 0; c < CL_K0; c += 2)
-        *reinterpret_cast<u32*>(xs + lane * S80 + c) = pack_bf16(f[c], f[c + 1]);
-      spatch[lane] = S;
+      for (int k = 0; k < CL_K0; ++k) f[k] = 0.f;
     }
-    __syncwarp();
-    u32 x0[5][4];
-#pragma unroll
-    for (int ks = 0; ks < 5; ++ks) ld_a(x0[ks], xs, S80, 0, ks * 16, g, t);
-    float y[4], z1[8][4], z2[8][4], z3[8][4];
-    u32 a1[4][4], a2[4][4], a3[4][4];
-    mlp_forward<false>(s, x0, y, z1, z2, z3, a1, a2, a3, g, t);
-    // y: rows g, g+8; columns 2t, 2t+1 (outputs 0..2 live in t = 0, 1)
-    if (t < 2) {
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int r = g + 8 * h, i = r0 + r;
-        if (i < n) {
-          const float sc = spatch[r] * rm.out_scale;
-          float* a = reinterpret_cast<float*>(&acc[i]);
-          a[2 * t] += y[2 * h] * sc;
-          if (t == 0) a[1] += y[2 * h + 1] * sc;
-        }
-      }
+    tc_store_row<CL_K0 / 8>(xb, threadIdx.x, TC_KX, f);
+    float y[3];
+    tc_forward(s, phase, err, y);
+    if (i < n) {
+      const float sc = S * rm.out_scale;
+      float4 a = acc[i];
+      a.x += y[0] * sc;
+      a.y += y[1] * sc;
+      a.z += y[2] * sc;
+      acc[i] = a;
     }
-    __syncwarp();
   }
+  tc_teardown(s);
 }
 
 // ------------------------------------------------------------------ training ---------
@@ -570,42 +775,35 @@ __global__ void features_kernel(const float* __restrict__ pos, int n, ReducedMes
   spatch[i] = S;
 }
 
-// MLP on given inputs (test support): X float [n][67] -> Y [n][3]
-__global__ void __launch_bounds__(CL_THREADS) mlp_eval_kernel(const float* __restrict__ X, int n,
+// MLP on given inputs (test support, the inference path): X float [n][67] -> Y [n][3]
+__global__ void __launch_bounds__(TC_THREADS) mlp_eval_kernel(const float* __restrict__ X, int n,
                                                               const bf16* __restrict__ img,
                                                               const float* __restrict__ params,
-                                                              float* __restrict__ Y) {
+                                                              float* __restrict__ Y, int* __restrict__ err) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemMLP& s = *reinterpret_cast<SmemMLP*>(smem_raw);
-  bf16* xs_all = reinterpret_cast<bf16*>(smem_raw + sizeof(SmemMLP));
-  load_mlp_smem(s, img, params);
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  bf16* xs = xs_all + warp * 16 * S80;
-  const int tiles = (n + 15) / 16;
-  for (int tile = blockIdx.x * CL_WARPS + warp; tile < tiles; tile += gridDim.x * CL_WARPS) {
-    const int r0 = tile * 16;
-    for (int e = lane; e < 16 * CL_K0; e += 32) {
-      const int r = e / CL_K0, c = e % CL_K0, i = r0 + r;
-      xs[r * S80 + c] = __float2bfloat16_rn(i < n && c < CL_IN ? X[(size_t)i * CL_IN + c] : 0.f);
-    }
-    __syncwarp();
-    u32 x0[5][4];
+  TcSmem& s = *reinterpret_cast<TcSmem*>(smem_raw);
+  tc_setup(s, img, params);
+  unsigned char* xb = reinterpret_cast<unsigned char*>(s.x);
+  u32 phase = 0;
+  const int tiles = (n + TC_ROWS - 1) / TC_ROWS;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const int i = tile * TC_ROWS + threadIdx.x;
+    float f[CL_K0];
 #pragma unroll
-    for (int ks = 0; ks < 5; ++ks) ld_a(x0[ks], xs, S80, 0, ks * 16, g, t);
-    float y[4], z1[8][4], z2[8][4], z3[8][4];
-    u32 a1[4][4], a2[4][4], a3[4][4];
-    mlp_forward<false>(s, x0, y, z1, z2, z3, a1, a2, a3, g, t);
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const int r = g + 8 * (e >> 1), o = 2 * t + (e & 1), i = r0 + r;
-      if (i < n && o < 3) Y[(size_t)i * 3 + o] = y[e];
+    for (int k = 0; k < CL_K0; ++k) f[k] = (i < n && k < CL_IN) ? X[(size_t)i * CL_IN + k] : 0.f;
+    tc_store_row<CL_K0 / 8>(xb, threadIdx.x, TC_KX, f);
+    float y[3];
+    tc_forward(s, phase, err, y);
+    if (i < n) {
+      Y[(size_t)i * 3 + 0] = y[0];
+      Y[(size_t)i * 3 + 1] = y[1];
+      Y[(size_t)i * 3 + 2] = y[2];
     }
-    __syncwarp();
   }
+  tc_teardown(s);
 }
 
-constexpr size_t kInferSmem = sizeof(SmemMLP) + CL_WARPS * 16 * S80 * sizeof(bf16) + CL_WARPS * 16 * sizeof(float);
+constexpr size_t kInferSmem = sizeof(TcSmem);
 constexpr size_t kTrainSmem = sizeof(SmemMLP) + CL_WARPS * sizeof(TrainSmemWarp);
 
 static int configure_closure_kernels() {
@@ -685,11 +883,13 @@ int closure_apply(pmgb_pm* h) {
   if (!c || c->mode != PMGB_CLOSURE_LEARNED) return PMGB_OK;
   int rc = occupancy(c, h->pm[h->cur], h->n);
   if (rc) return rc;
-  const int tiles = (h->n + 15) / 16;
-  const int blocks = std::min((tiles + CL_WARPS - 1) / CL_WARPS, h->num_sms * 4);
+  // 128-particle tiles; ~67 KB of shared memory and 64 TMEM columns per CTA: 3 CTAs per SM
+  const int tiles = (h->n + TC_ROWS - 1) / TC_ROWS;
+  const int blocks = std::min(tiles, h->num_sms * 3);
   if (blocks > 0) {
-    closure_infer_kernel<<<blocks, CL_THREADS, kInferSmem, h->st>>>(h->pm[h->cur], h->n, c->rm, c->occ, c->img,
-                                                                    c->params, h->acc_pm, h->flags);
+    closure_infer_kernel<<<blocks, TC_THREADS, kInferSmem, h->st>>>(h->pm[h->cur], h->n, c->rm, c->occ, c->img,
+                                                                    c->params, h->acc_pm, h->flags,
+                                                                    h->flags + kFlagTimeout);
     PMGB_LAUNCH_CHECK();
     count_launches(1);
   }
@@ -1032,22 +1232,30 @@ int pmgb_mlp_eval(const float* params, int n, const float* x, float* y) {
   if (rc) return rc;
   float *dp = nullptr, *dx = nullptr, *dy = nullptr;
   bf16* img = nullptr;
+  int* derr = nullptr;
   const size_t nn = (size_t)std::max(n, 1);
   PMGB_CUDA_TRY(cudaMalloc(&dp, CL_NPARAM * sizeof(float)));
   PMGB_CUDA_TRY(cudaMalloc(&img, IMG_SIZE * sizeof(bf16)));
   PMGB_CUDA_TRY(cudaMalloc(&dx, nn * CL_IN * sizeof(float)));
   PMGB_CUDA_TRY(cudaMalloc(&dy, nn * 3 * sizeof(float)));
+  PMGB_CUDA_TRY(cudaMalloc(&derr, sizeof(int)));
   cudaMemcpy(dp, params, CL_NPARAM * sizeof(float), cudaMemcpyHostToDevice);
   cudaMemcpy(dx, x, (size_t)n * CL_IN * sizeof(float), cudaMemcpyHostToDevice);
+  cudaMemset(derr, 0, sizeof(int));
   image_kernel<<<64, 256>>>(dp, img);
-  mlp_eval_kernel<<<std::max(1, std::min(1024, (n + 63) / 64)), CL_THREADS, kInferSmem>>>(dx, n, img, dp, dy);
+  mlp_eval_kernel<<<std::max(1, std::min(1024, (n + TC_ROWS - 1) / TC_ROWS)), TC_THREADS, kInferSmem>>>(
+      dx, n, img, dp, dy, derr);
   cudaMemcpy(y, dy, (size_t)n * 3 * sizeof(float), cudaMemcpyDeviceToHost);
+  int timed_out = 0;
+  cudaMemcpy(&timed_out, derr, sizeof(int), cudaMemcpyDeviceToHost);
   cudaError_t err = cudaDeviceSynchronize();
   cudaFree(dp);
   cudaFree(img);
   cudaFree(dx);
   cudaFree(dy);
+  cudaFree(derr);
   if (err != cudaSuccess) return set_error(cudaGetErrorString(err)), PMGB_ECUDA;
+  if (timed_out) return set_error("a tensor-core wait gave up"), PMGB_ETIMEOUT;
   return PMGB_OK;
 }
 

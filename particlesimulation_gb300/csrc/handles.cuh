@@ -46,6 +46,12 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
 
 }  // namespace pmgb
 
+namespace pmgb {
+// word of pmgb_pm::flags that a kernel sets when a bounded device wait gave up (the run then
+// returns PMGB_ETIMEOUT)
+constexpr int kFlagTimeout = 2;
+}  // namespace pmgb
+
 struct pmgb_p3m;
 struct pmgb_closure;
 struct pmgb_diag;
@@ -71,7 +77,7 @@ struct pmgb_pm {
   float* ghat = nullptr;
   float2* tw = nullptr;
   int nmax = 0;
-  int* flags = nullptr;  // device: [0] stop, [1] escape iteration
+  int* flags = nullptr;  // device: [0] stop, [1] escape iteration, [kFlagTimeout] a wait gave up
   pmgb_p3m* p3m = nullptr;
   pmgb_closure* closure = nullptr;  // learned short-range closure applied after interpolation
   int since_sort = 1 << 30;
