@@ -337,6 +337,10 @@ int pmgb_closure_scales(pmgb_closure* c, float* out_scale, int* dims3);
 int pmgb_mlp_eval(const float* params, int n, const float* x, float* y);
 int pmgb_mlp_gradients(const float* params, int n, const float* x, const float* t, float* grad,
                        float* loss);
+/* Test support: the bounded mbarrier wait of the tensor-core kernels, on a barrier that gets its
+ * one arrival (arrive = 1: PMGB_OK) or none (arrive = 0: the wait gives up after `spins` tries
+ * and the call returns PMGB_ETIMEOUT, the device context still usable). */
+int pmgb_tc_wait_probe(int arrive, int spins);
 
 /* Chaining-mesh cell lists built without allocating any device memory.  No counterpart in the
  * reference: it is for callers that cannot allocate device memory where they need the lists

@@ -31,6 +31,7 @@ EXPORTS = [
     "pmgb_closure_collect", "pmgb_closure_train", "pmgb_closure_param_count",
     "pmgb_closure_get_params", "pmgb_closure_set_params", "pmgb_closure_judge", "pmgb_closure_run",
     "pmgb_closure_features", "pmgb_closure_scales", "pmgb_mlp_eval", "pmgb_mlp_gradients",
+    "pmgb_tc_wait_probe",
     "pmgb_ensemble_create", "pmgb_ensemble_destroy", "pmgb_ensemble_run", "pmgb_ensemble_advance",
     "pmgb_ensemble_get_particles", "pmgb_ensemble_tuning", "pmgb_ensemble_size",
     "pmgb_last_error", "pmgb_version",
@@ -127,6 +128,7 @@ def lib() -> C.CDLL:
         L.pmgb_closure_scales.argtypes = [vp, fp, ip]
         L.pmgb_mlp_eval.argtypes = [fp, C.c_int, fp, fp]
         L.pmgb_mlp_gradients.argtypes = [fp, C.c_int, fp, fp, fp, fp]
+        L.pmgb_tc_wait_probe.argtypes = [C.c_int, C.c_int]
         L.pmgb_ensemble_create.argtypes = [C.c_int, C.POINTER(PMConfigC), ip, C.POINTER(fp),
                                            C.POINTER(fp), C.POINTER(vp)]
         L.pmgb_ensemble_destroy.argtypes = [vp]

@@ -319,9 +319,9 @@ __device__ __forceinline__ void tc_mma_layer(u32 tmem, u32 a, u32 akstride, u32 
 }
 
 // bounded wait for the mbarrier phase of the given parity; false if it gave up
-__device__ __forceinline__ bool tc_wait(u32 mbar, u32 parity) {
+__device__ __forceinline__ bool tc_wait(u32 mbar, u32 parity, int spins = TC_WAIT_SPINS) {
   u32 done = 0;
-  for (int it = 0; it < TC_WAIT_SPINS && !done; ++it) {
+  for (int it = 0; it < spins && !done; ++it) {
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
         " selp.u32 %0, 1, 0, p;\n}\n"
@@ -1256,6 +1256,33 @@ int pmgb_mlp_eval(const float* params, int n, const float* x, float* y) {
   cudaFree(derr);
   if (err != cudaSuccess) return set_error(cudaGetErrorString(err)), PMGB_ECUDA;
   if (timed_out) return set_error("a tensor-core wait gave up"), PMGB_ETIMEOUT;
+  return PMGB_OK;
+}
+
+// Test support: the tensor-core path's bounded mbarrier wait on a barrier of one expected
+// arrival that gets it (arrive = 1) or never does (arrive = 0).
+__global__ void tc_wait_probe_kernel(int arrive, int spins, int* __restrict__ err) {
+  __shared__ __align__(8) u64 mbar;
+  const u32 a = smem_addr(&mbar);
+  if (threadIdx.x == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(a) : "memory");
+  __syncthreads();
+  if (threadIdx.x == 0 && arrive)
+    asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" :: "r"(a) : "memory");
+  if (!tc_wait(a, 0u, spins)) atomicExch(err, 1);
+}
+
+int pmgb_tc_wait_probe(int arrive, int spins) {
+  if (spins < 1) return set_error("spins must be positive"), PMGB_EINVAL;
+  int* derr = nullptr;
+  PMGB_CUDA_TRY(cudaMalloc(&derr, sizeof(int)));
+  int gave_up = 0;
+  cudaMemset(derr, 0, sizeof(int));
+  tc_wait_probe_kernel<<<1, TC_THREADS>>>(arrive, spins, derr);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(&gave_up, derr, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(derr);
+  if (e != cudaSuccess) return set_error(cudaGetErrorString(e)), PMGB_ECUDA;
+  if (gave_up) return set_error("a bounded device wait gave up"), PMGB_ETIMEOUT;
   return PMGB_OK;
 }
 

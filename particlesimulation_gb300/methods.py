@@ -584,6 +584,12 @@ def mlp_eval(params, x):
     return y
 
 
+def tc_wait_probe(arrive, spins):
+    """Status code of the tensor-core kernels' bounded mbarrier wait on a barrier that gets its
+    arrival (arrive=True) or never does: PMGB_OK or PMGB_ETIMEOUT (returned, not raised)."""
+    return lib().pmgb_tc_wait_probe(1 if arrive else 0, int(spins))
+
+
 def mlp_gradients(params, x, t):
     """Gradient of mean_rows |MLP(x) - t|^2 w.r.t. the parameters, by our training kernels."""
     p = _f32(params).reshape(-1)

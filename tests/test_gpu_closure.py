@@ -135,3 +135,17 @@ def test_judge_falls_back_to_plain_p3m(gpu_lib):
     assert cl.mode() == cl.FULL
     cl.close()
     pm.close()
+
+
+def test_tensor_core_wait_gives_up_and_context_survives(gpu_lib):
+    """The bounded mbarrier wait of the tcgen05 kernels: with its arrival it completes; on a
+    barrier nothing arrives on it gives up after its spin bound and the call reports
+    PMGB_ETIMEOUT; the context stays usable (the tensor-core MLP runs correctly afterwards)."""
+    from particlesimulation_gb300 import _lib, methods
+    assert methods.tc_wait_probe(True, 1 << 20) == _lib.PMGB_OK
+    assert methods.tc_wait_probe(False, 2000) == _lib.PMGB_ETIMEOUT
+    p = M.init_params(5)
+    x = np.random.default_rng(1).uniform(-1, 1, (300, M.IN)).astype(np.float32)
+    y = methods.mlp_eval(p, x)
+    want, _ = M.forward(p, x, bf16=True)
+    assert np.sqrt(((y - want) ** 2).mean() / (want ** 2).mean()) < 3e-3
