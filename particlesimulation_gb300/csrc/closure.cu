@@ -259,8 +259,10 @@ __device__ __forceinline__ float features(const ReducedMesh& rm, const float* __
 // no-swizzle K-major layout: 8-row x 16-byte core matrices, the core matrix of row group g and
 // K group j at j * kstride + g * 128 bytes; the matrix descriptor's leading byte offset is the
 // K-group stride, the stride byte offset the row-group stride.  Every wait on the mbarrier is
-// bounded; a wait that gives up sets err[0] and the kernel runs on to its end (uniform control
-// flow), and the host reports PMGB_ETIMEOUT.  Training keeps the mma.sync kernels above.
+// bounded (1 s of %globaltimer, and a poll count); a wait that gives up sets err[0], the thread
+// waits no more and thread 0 issues no more MMAs, while the barriers stay where they are, so
+// the kernel reaches its end (and frees its TMEM) and the host reports PMGB_ETIMEOUT.
+// Training keeps the mma.sync kernels above.
 constexpr int TC_ROWS = 128;
 constexpr int TC_THREADS = 128;
 constexpr int TC_N4 = 16;                   // output layer, padded
@@ -268,7 +270,8 @@ constexpr int TC_COLS = 64;                 // TMEM columns (power of two >= 32)
 constexpr u32 TC_KX = TC_ROWS * 16;         // K-group stride of the 128-row A operands (bytes)
 constexpr u32 TC_KW = CL_H * 16;            // K-group stride of the 64-row weight operands
 constexpr u32 TC_KW4 = TC_N4 * 16;          // K-group stride of the output layer's weights
-constexpr int TC_WAIT_SPINS = 1 << 24;      // bound of an mbarrier wait (far beyond a layer's MMAs)
+constexpr int TC_WAIT_SPINS = 1 << 24;      // backstop of an mbarrier wait's polls
+constexpr unsigned long long TC_WAIT_NS = 1000000000ull;  // bound of an mbarrier wait: 1 s
 
 struct TcSmem {
   alignas(16) bf16 w1[CL_H * CL_K0];
@@ -318,10 +321,19 @@ __device__ __forceinline__ void tc_mma_layer(u32 tmem, u32 a, u32 akstride, u32 
                :: "r"(mbar) : "memory");
 }
 
-// bounded wait for the mbarrier phase of the given parity; false if it gave up
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wait for the mbarrier phase of the given parity, for at most TC_WAIT_NS nanoseconds and
+// `spins` polls; false if it gave up.
 __device__ __forceinline__ bool tc_wait(u32 mbar, u32 parity, int spins = TC_WAIT_SPINS) {
   u32 done = 0;
+  const unsigned long long t0 = globaltimer_ns();
   for (int it = 0; it < spins && !done; ++it) {
+    if ((it & 255) == 255 && globaltimer_ns() - t0 > TC_WAIT_NS) break;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
         " selp.u32 %0, 1, 0, p;\n}\n"
@@ -420,8 +432,11 @@ __device__ void tc_setup(TcSmem& s, const bf16* __restrict__ img, const float* _
 }
 
 // Forward pass of one tile whose inputs are in s.x: returns this thread's row of the output
-// layer (3 values).  phase: the mbarrier parity of the next commit (advanced by 4).
-__device__ __forceinline__ void tc_forward(TcSmem& s, u32& phase, int* __restrict__ err, float y[3]) {
+// layer (3 values).  phase: the mbarrier parity of the next commit (advanced by 4).  live: false
+// once one of this thread's waits gave up; from then on the thread waits no more (thread 0 also
+// issues no more MMAs), so a failed launch ends within about one wait bound, err[0] set.
+__device__ __forceinline__ void tc_forward(TcSmem& s, u32& phase, bool& live, int* __restrict__ err,
+                                           float y[3]) {
   const u32 tmem = s.tmem;
   const u32 taddr = tmem + ((u32)(threadIdx.x & ~31) << 16);
   const u32 mbar = smem_addr(&s.mbar);
@@ -434,10 +449,13 @@ __device__ __forceinline__ void tc_forward(TcSmem& s, u32& phase, int* __restric
   __syncthreads();
 #pragma unroll 1
   for (int l = 0; l < 3; ++l) {
-    if (threadIdx.x == 0)
+    if (threadIdx.x == 0 && live)
       tc_mma_layer(tmem, l == 0 ? xa : ha, TC_KX, wa[l], TC_KW, l == 0 ? CL_K0 / 16 : CL_H / 16,
                    tc_idesc(TC_ROWS, CL_H), mbar);
-    if (!tc_wait(mbar, phase & 1u)) atomicExch(err, 1);
+    if (live && !tc_wait(mbar, phase & 1u)) {
+      live = false;
+      atomicExch(err, 1);
+    }
     ++phase;
     float z[64];
     tc_ld64(taddr, z);
@@ -449,9 +467,12 @@ __device__ __forceinline__ void tc_forward(TcSmem& s, u32& phase, int* __restric
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
   }
-  if (threadIdx.x == 0)
+  if (threadIdx.x == 0 && live)
     tc_mma_layer(tmem, ha, TC_KX, smem_addr(s.w4), TC_KW4, CL_H / 16, tc_idesc(TC_ROWS, TC_N4), mbar);
-  if (!tc_wait(mbar, phase & 1u)) atomicExch(err, 1);
+  if (live && !tc_wait(mbar, phase & 1u)) {
+    live = false;
+    atomicExch(err, 1);
+  }
   ++phase;
   float o[16];
   tc_ld16(taddr, o);
@@ -484,6 +505,7 @@ __global__ void __launch_bounds__(TC_THREADS) closure_infer_kernel(
   tc_setup(s, img, params);
   unsigned char* xb = reinterpret_cast<unsigned char*>(s.x);
   u32 phase = 0;
+  bool live = true;
   const int tiles = (n + TC_ROWS - 1) / TC_ROWS;
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     const int i = tile * TC_ROWS + threadIdx.x;
@@ -498,7 +520,7 @@ __global__ void __launch_bounds__(TC_THREADS) closure_infer_kernel(
     }
     tc_store_row<CL_K0 / 8>(xb, threadIdx.x, TC_KX, f);
     float y[3];
-    tc_forward(s, phase, err, y);
+    tc_forward(s, phase, live, err, y);
     if (i < n) {
       const float sc = S * rm.out_scale;
       float4 a = acc[i];
@@ -785,6 +807,7 @@ __global__ void __launch_bounds__(TC_THREADS) mlp_eval_kernel(const float* __res
   tc_setup(s, img, params);
   unsigned char* xb = reinterpret_cast<unsigned char*>(s.x);
   u32 phase = 0;
+  bool live = true;
   const int tiles = (n + TC_ROWS - 1) / TC_ROWS;
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     const int i = tile * TC_ROWS + threadIdx.x;
@@ -793,7 +816,7 @@ __global__ void __launch_bounds__(TC_THREADS) mlp_eval_kernel(const float* __res
     for (int k = 0; k < CL_K0; ++k) f[k] = (i < n && k < CL_IN) ? X[(size_t)i * CL_IN + k] : 0.f;
     tc_store_row<CL_K0 / 8>(xb, threadIdx.x, TC_KX, f);
     float y[3];
-    tc_forward(s, phase, err, y);
+    tc_forward(s, phase, live, err, y);
     if (i < n) {
       Y[(size_t)i * 3 + 0] = y[0];
       Y[(size_t)i * 3 + 1] = y[1];
