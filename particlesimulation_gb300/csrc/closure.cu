@@ -1089,7 +1089,6 @@ int pmgb_closure_train(pmgb_closure* c, int epochs, int batch, float lr, float* 
   const int steps_per_epoch = c->count / batch;
   const int total_steps = epochs * steps_per_epoch;
   float last = 0.f;
-  double epoch_loss = 0.0;
   int step = 0;
   for (int e = 0; e < epochs; ++e) {
     for (int i = 0; i < c->count; ++i) hp[i] = i;
@@ -1098,7 +1097,6 @@ int pmgb_closure_train(pmgb_closure* c, int epochs, int batch, float lr, float* 
       cudaFree(perm);
       return set_error("permutation upload failed"), PMGB_ECUDA;
     }
-    epoch_loss = 0.0;
     for (int b = 0; b < steps_per_epoch; ++b, ++step) {
       const int nw = batch / 16;
       closure_train_kernel<<<nw / CL_WARPS, CL_THREADS, kTrainSmem, st>>>(
