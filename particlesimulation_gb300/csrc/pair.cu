@@ -233,7 +233,11 @@ __global__ void __launch_bounds__(PAIR_THREADS) pair_kernel(
 //  * the table is replicated 16 times, copy (lane mod 16) for each lane, so the per-lane lookups
 //    of a half warp fall into 16 distinct bank pairs whatever their segments (an 8-byte load
 //    of a warp then takes the minimum of two shared-memory wavefronts instead of about four);
-//    64 KB of shared memory, hence 512-thread CTAs to keep 32 warps per SM.
+//    64 KB of shared memory;
+//  * one 512-thread CTA per SM with the whole register file, 128 registers per thread
+//    (SLOT_CTAS_PER_SM): two CTAs of 64 registers (32 warps per SM) spilled and took 6.42 ms on
+//    the 262,144-particle disk; one CTA (16 warps, enough to keep issue busy with the 16-deep
+//    candidate loop) took 6.51 ms at 80 registers, 6.23 at 96, 6.36 at 112, 6.18 at 128.
 // The y window of the slice in the neighbour's y-sorted list is found by a warp-cooperative
 // search (32 probes per round).  Per-chunk partial sums are added with Kahan compensation.
 constexpr int SLOT_IPL = 2;                  // i particles per lane
@@ -243,6 +247,7 @@ constexpr int SLOT_REP = 16;                 // table copies (lane mod 16)
 constexpr int NNB = 27;                      // neighbour cells (and slots) per particle
 constexpr int SLOT_THREADS = 512;
 constexpr int SLOT_WARPS = SLOT_THREADS / 32;
+constexpr int SLOT_CTAS_PER_SM = 1;         // resident CTAs per SM (128 registers per thread)
 // staging (SLOT_WARPS x 32 float4) + CTA partial sums (SLOT_WARPS x SLOT_SLICE float4) + table
 constexpr int SLOT_SMEM = SLOT_WARPS * 32 * 16 + SLOT_WARPS * SLOT_SLICE * 16 + SLOT_TAB * SLOT_REP * 8;
 // Units whose estimated cost reaches 1/SLOT_HEAVY_DIV of a warp's share of the pass (and at
@@ -467,7 +472,7 @@ __device__ __forceinline__ void slot_unit(const SlotCtx& c, u32 it, float4 (*jbu
 // far end of the same buffer, counter[1]), then the rest in unit order (counter[8]).  If the
 // lists overflowed the buffer, every unit is taken by the last loop.
 template <bool EQM>
-__global__ void __launch_bounds__(SLOT_THREADS) pair_slot_kernel(
+__global__ void __maxnreg__(128) pair_slot_kernel(
     const float4* __restrict__ pm, int n, const int* __restrict__ cell_start,
     const int2* __restrict__ items, const u32* __restrict__ nitems_p, const u32* __restrict__ heavy,
     u32 heavy_cap, u32* __restrict__ counter, ChainDimsP cd, PairParams pp, const float* __restrict__ table,
@@ -664,11 +669,11 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
     const int pb = (nitems_max + 255) / 256;
     plan_cost_kernel<<<pb, 256, 0, st>>>(cell_start, items, nitems, cd, counter, stop);
     plan_heavy_kernel<<<pb, 256, 0, st>>>(cell_start, items, nitems, cd, heavy, heavy_cap, counter,
-                                          (unsigned long long)num_sms * 2 * SLOT_WARPS, stop);
+                                          (unsigned long long)num_sms * SLOT_CTAS_PER_SM * SLOT_WARPS, stop);
   }
   if (ev_pair) PMGB_CUDA_TRY(cudaEventRecord(ev_pair, st));
   const dim3 grid(num_sms * 8), block(PAIR_THREADS);
-  if (slotted) {  // table, staging and partial sums: 86.5 KB of dynamic shared memory
+  if (slotted) {  // table, staging and partial sums: 88.1 KB of dynamic shared memory
     PMGB_CUDA_TRY(cudaFuncSetAttribute(pair_slot_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SLOT_SMEM));
     PMGB_CUDA_TRY(cudaFuncSetAttribute(pair_slot_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SLOT_SMEM));
   }
@@ -678,10 +683,10 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
   if (slotted) {
     if (nitems_max > 0) launches += 2;  // the two planning kernels
     if (equal_mass)
-      pair_slot_kernel<true><<<num_sms * 2, SLOT_THREADS, SLOT_SMEM, st>>>(
+      pair_slot_kernel<true><<<num_sms * SLOT_CTAS_PER_SM, SLOT_THREADS, SLOT_SMEM, st>>>(
           pm, n, cell_start, items, nitems, heavy, heavy_cap, counter, cd, pp, table, slots, stop);
     else
-      pair_slot_kernel<false><<<num_sms * 2, SLOT_THREADS, SLOT_SMEM, st>>>(
+      pair_slot_kernel<false><<<num_sms * SLOT_CTAS_PER_SM, SLOT_THREADS, SLOT_SMEM, st>>>(
           pm, n, cell_start, items, nitems, heavy, heavy_cap, counter, cd, pp, table, slots, stop);
     if (n > 0)
       pair_epilogue_kernel<<<(n + 255) / 256, 256, 0, st>>>(pm, vi, acc_pm, slots, n, sp, kick, drift,
