@@ -420,8 +420,9 @@ __device__ __forceinline__ void slot_unit(const SlotCtx& c, u32 it, float4 (*jbu
         const int cnt = min(32, e - j0);
 #pragma unroll
         for (int u = 0; u < SLOT_IPL; ++u) I[u].px = I[u].py = I[u].pz = 0.f;
-        // unrolled 16 deep (32 independent pair chains per lane in flight; 6.62 ms at 4, 6.53
-        // at 8, 6.42 at 16 on the 262,144-particle disk)
+        // unrolled 16 deep (32 independent pair chains per lane in flight; two bodies cover a full
+        // chunk): on the 262,144-particle disk 6.23 ms at 8, 6.17 at 16, 6.29 at 32 and 6.8 at
+        // 24 (remainder iterations)
 #pragma unroll 16
         for (int s = 0; s < cnt; ++s) {
           const float4 q = jbuf[warp][s];
