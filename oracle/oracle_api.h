@@ -15,7 +15,7 @@
  *
  * Nothing in the product (particlesimulation_gb300/, include/) links or calls these.
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs use them, and
- * only as the checker / the timed CPU baseline.
+ * only as the reference results / the timed CPU baseline.
  *
  * Units follow the reference: inputs are in "original" units (state = N positions then N
  * velocities, each xyz float triplets); accelerations are returned in code units

@@ -1,7 +1,7 @@
 /*
  * port.cpp - CPU restatement of the reference's PM / P3M force-and-step path.
  * TEST INFRASTRUCTURE ONLY ("the oracle"): tests/, __graft_entry__.smoke() and bench.py's
- * CPU-baseline legs call it as the checker or as the timed CPU baseline; the product
+ * CPU-baseline legs call it as the reference results or as the timed CPU baseline; the product
  * (particlesimulation_gb300/, include/) never links it.
  *
  * Everything is templated on the scalar type T.  T = float repeats the reference's FP32

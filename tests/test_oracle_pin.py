@@ -1,4 +1,4 @@
-"""Pins the CPU oracle (oracle/port.cpp) before it is trusted as the checker.
+"""Pins the CPU oracle (oracle/port.cpp) before its results are trusted in the parity tests.
 
 Two pins: (1) against the golden fixtures generated from the reference's own CPU code
 (tests/golden/make_golden.py) - always runs; (2) directly against the reference compiled from
