@@ -159,6 +159,11 @@ int pmgb_pm_stage_times(pmgb_pm* pm, float* ms5);
 /* Number of particles and the grid of a handle. */
 int pmgb_pm_size(pmgb_pm* pm, int* n, int* grid3);
 
+/* The handle's CUDA stream (a cudaStream_t), on which every call of the handle and of the P3M /
+ * closure handles over it enqueues its work; for callers that time or order their own work
+ * against it.  No reference counterpart (the reference's GPU path uses the default stream). */
+int pmgb_pm_get_stream(pmgb_pm* pm, void** stream);
+
 /* ---------------------------------------------------------------- run diagnostics ---- */
 
 /* What PMMethod::run / P3MMethod::run(..., collectDiagnostics = true) record once per loop
@@ -356,6 +361,17 @@ int pmgb_tc_wait_probe(int arrive, int spins);
 int pmgb_chaining_mesh_fill_noalloc(const float* d_pos, int n, const pmgb_p3m_config* cfg,
                                     float H, int* d_order, int* d_counts, int* dims3,
                                     void* stream);
+
+/* ---------------------------------------------------------------- direct sum -------- */
+/* ppMethod's pairwise gravitational acceleration (source/ppMethod.cpp:23-36) restated in FP64
+ * on the device, for the m targets idx[0..m) against all n particles: acc[3k..3k+2] =
+ * sum_{j != idx[k]} -G m_j (x_i - x_j) / (|x_i - x_j|^2 + eps^2)^1.5.  pos = n xyz triplets and
+ * masses (host, any consistent units); acc = m xyz triplets (host, double).  periodic_L > 0:
+ * minimum-image separations in a cube of that side (no Ewald sum).  The yardstick of the force
+ * error reports (the reference uses its PP integrator the same way in its accuracy scenarios,
+ * source/demos.cpp:390-396, 617-621); deterministic (fixed summation order). */
+int pmgb_direct_sum_fp64(int n, const float* pos, const float* masses, double G, double eps, int m,
+                         const int* idx, double periodic_L, double* acc);
 
 /* ---------------------------------------------------------------- misc -------------- */
 /* FP32 FMA throughput of the current device in TFLOP/s, measured by a timed FMA kernel (the

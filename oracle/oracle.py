@@ -376,16 +376,23 @@ def port_sr_table(q: P3MConfig, H):
 
 
 def port_time_steps(cfg: PMConfig, q: P3MConfig | None, pos, vel, mass, steps, nthreads,
-                    pair_stride=1):
-    """Seconds per step of the port in float: dict(est, pm, cells, pair_sampled)."""
+                    pair_stride=1, fill_stride=1):
+    """Seconds per step of the port in float: dict(est, pm, cells, pair_sampled, wall).
+
+    pair_stride S: only every S-th particle (by index) is an i-particle of the pair pass (its
+    time is scaled by S in ``est``); fill_stride F: the reference's y-sorting insertion sort runs
+    on every F-th particle and its time is scaled by F^2 (``cells`` is the scaled figure).
+    ``wall`` is the time the sampled steps actually took, per step."""
     n = len(mass)
     st, m = _state(pos, vel), _f32(mass)
     out = np.zeros(4, np.float64)
-    rc = port().port_time_steps(C.byref(cfg.c()), C.byref(q.c()) if q is not None else None, n,
-                                _ptr(st, C.c_float), _ptr(m, C.c_float), steps, nthreads,
-                                pair_stride, _ptr(out, C.c_double))
+    wall = C.c_double(0)
+    rc = port().port_time_steps2(C.byref(cfg.c()), C.byref(q.c()) if q is not None else None, n,
+                                 _ptr(st, C.c_float), _ptr(m, C.c_float), steps, nthreads,
+                                 pair_stride, fill_stride, _ptr(out, C.c_double), C.byref(wall))
     assert rc == 0
-    return dict(est=out[0], pm=out[1], cells=out[2], pair_sampled=out[3])
+    return dict(est=out[0], pm=out[1], cells=out[2], pair_sampled=out[3],
+                wall=wall.value / max(steps, 1))
 
 
 # ----------------------------------------------------------------- samplers ---

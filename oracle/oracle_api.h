@@ -124,6 +124,13 @@ int port_sr_table(const orc_p3m_params* q, float H, float* table /*500*/, float*
 int port_time_steps(const orc_pm_params* p, const orc_p3m_params* q, int n,
                     const float* state, const float* masses, int steps, int nthreads,
                     int pair_stride, double* out4);
+/* port_time_steps with the y-sorted cell-list build sampled too: fill_stride F > 1 times the
+ * reference's insertion sort on every F-th particle and scales it by F^2 (its cost is quadratic
+ * in the cell populations); the pair pass then runs on the complete lists built by an
+ * equivalent stable sort (untimed).  *wall (may be NULL) = seconds the call's steps took. */
+int port_time_steps2(const orc_pm_params* p, const orc_p3m_params* q, int n,
+                     const float* state, const float* masses, int steps, int nthreads,
+                     int pair_stride, int fill_stride, double* out4, double* wall);
 
 #ifdef __cplusplus
 }

@@ -42,6 +42,7 @@
 #include <algorithm>
 #include <array>
 #include <atomic>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <complex>
@@ -295,7 +296,8 @@ T greenValue(const orc_pm_params* p, T diameterCode, int kx, int ky, int kz) {
     return T(-1) / (fx * fx + fy * fy + fz * fz);
   }
   int cs = p->gf == 1 ? 0 : 1;
-  return greenOptimal<T>(p->is, kx, ky, kz, nx, ny, nz, diameterCode, cs, p->fds);
+  // is = 3 (centred TSC, a deviation from the reference) has TSC's assignment function
+  return greenOptimal<T>(p->is == 3 ? 2 : p->is, kx, ky, kz, nx, ny, nz, diameterCode, cs, p->fds);
 }
 
 /* ------------------------------------------------------------------- PM ---- */
@@ -374,6 +376,22 @@ struct PM {
       }
     });
   }
+  // TSC's centre cell.  The reference (is = 2) centres the 3-point stencil on the cell below
+  // the particle (int(x), offsets in [0, 1): pmMethod.cpp:250-270, 312-331), so its weights
+  // (TSCAssignmentFunc, pmMethod.cpp:187-198) jump where x crosses an integer and go negative
+  // above sqrt(3)/2.  is = 3 (a deviation, not in the reference) centres it on the nearest
+  // mesh point, offsets in [-1/2, 1/2]: the standard TSC of Hockney & Eastwood.
+  void tscBase(const V3<T>& q, int& ix, int& iy, int& iz) const {
+    if (p.is == 3) {
+      ix = (int)std::floor(q.x + T(0.5));
+      iy = (int)std::floor(q.y + T(0.5));
+      iz = (int)std::floor(q.z + T(0.5));
+    } else {
+      ix = (int)q.x;
+      iy = (int)q.y;
+      iz = (int)q.z;
+    }
+  }
   void spreadMass() {
     std::fill(dens.begin(), dens.end(), std::complex<T>(0, 0));
     for (int i = 0; i < N; ++i) {
@@ -395,7 +413,8 @@ struct PM {
         dens[idx(ix, iy + 1, iz + 1)] += d * tx * dy * dz;
         dens[idx(ix + 1, iy + 1, iz + 1)] += d * dx * dy * dz;
       } else {
-        int ix = (int)q.x, iy = (int)q.y, iz = (int)q.z;
+        int ix, iy, iz;
+        tscBase(q, ix, iy, iz);
         T d = m[i];
         T dx = q.x - ix, dy = q.y - iy, dz = q.z - iz;
         for (int t1 = -1; t1 <= 1; ++t1) {
@@ -437,6 +456,7 @@ struct PM {
       return fieldAt((int)std::round(q.x), (int)std::round(q.y), (int)std::round(q.z));
     }
     int xi = (int)q.x, yi = (int)q.y, zi = (int)q.z;
+    if (p.is >= 2) tscBase(q, xi, yi, zi);
     T dx = q.x - xi, dy = q.y - yi, dz = q.z - zi;
     if (p.is == 1) {
       T tx = 1 - dx, ty = 1 - dy, tz = 1 - dz;
@@ -542,6 +562,30 @@ struct ChainMesh {  // ChainingMesh (chainingMesh.cpp:6-84): linked lists over a
       }
     }
   }
+  // The lists fill(x, true) builds (ascending y, ties in index order), by a stable sort of each
+  // cell's particles instead of the reference's insertion sort (same order, O(n log n)); also
+  // kept as arrays (cellOrder[cellStart[c] .. cellStart[c+1])).
+  void fillSorted(const std::vector<V3<T>>& x) {
+    std::fill(hoc.begin(), hoc.end(), -1);
+    std::vector<std::vector<int>> cells(size);
+    for (int i = 0; i < int(x.size()); ++i) {
+      int c = cellOf(x[i]);
+      if (c >= 0) cells[c].push_back(i);
+    }
+    cellStart.assign(size + 1, 0);
+    cellOrder.clear();
+    for (int c = 0; c < size; ++c) {
+      auto& v = cells[c];
+      std::stable_sort(v.begin(), v.end(), [&](int a, int b) { return x[a].y < x[b].y; });
+      for (int k = int(v.size()) - 1; k >= 0; --k) {
+        next[v[k]] = hoc[c];
+        hoc[c] = v[k];
+      }
+      cellOrder.insert(cellOrder.end(), v.begin(), v.end());
+      cellStart[c + 1] = int(cellOrder.size());
+    }
+  }
+  std::vector<int> cellStart, cellOrder;
   void neighbors(int cell, int out[14]) const {
     int cx = cell % Mx, cy = (cell / Mx) % My, cz = cell / (Mx * My);
     int i = 0;
@@ -618,7 +662,44 @@ struct P3M {
     T F = mi * mj * (table[t] + (ksi - t) * (table[t + 1] - table[t]));
     return F * rij;
   }
-  int pairStride = 1;  // timing samples: only every pairStride-th particle of a list is an i
+  int pairStride = 1;  // timing samples: only every pairStride-th particle (by index) is an i
+  // Oracle runs (not the timed CPU baseline): y-sorted lists built by the equivalent stable sort,
+  // each j walk starting at the first particle with y >= y_i - re (the ones before it fail the
+  // cutoff test, as the reference's own early break assumes for the ones after the window), and
+  // cells taken by threads from a shared counter.  The pairs, their order per particle and every
+  // accumulator's writer are the reference's (sr[i] is written by i's cell only, slot[j][s] by
+  // the one cell whose neighbour s is j's cell), so the results are the same.
+  bool fast = false;
+  std::atomic<int> nextCell{0};
+  void fastJob() {
+    const auto& x = pm.x;
+    const auto& m = pm.m;
+    int nb[14];
+    for (int c = nextCell.fetch_add(1); c < cm.size; c = nextCell.fetch_add(1)) {
+      cm.neighbors(c, nb);
+      for (int s = 0; s < 14; ++s) {
+        const int cn = nb[s];
+        if (cn < 0) continue;
+        const int* jb = cm.cellOrder.data() + cm.cellStart[cn];
+        const int* je = cm.cellOrder.data() + cm.cellStart[cn + 1];
+        for (int k = cm.cellStart[c]; k < cm.cellStart[c + 1]; ++k) {
+          const int i = cm.cellOrder[k];
+          const T ylo = x[i].y - re;
+          const int* j0 = std::lower_bound(jb, je, ylo, [&](int j, T v) { return x[j].y < v; });
+          for (const int* pj = j0; pj < je; ++pj) {
+            const int j = *pj;
+            if (x[j].y - x[i].y > re) break;
+            if (i == j) continue;
+            V3<T> rij = x[i] - x[j];
+            if (mag2(rij) >= re * re) continue;
+            V3<T> f = srForce(rij, m[i], m[j]);
+            sr[i] += f;
+            if (cn != c) slot[j][s] += T(-1) * f;
+          }
+        }
+      }
+    }
+  }
   void threadJob(int tid, int threads) {
     const auto& x = pm.x;
     const auto& m = pm.m;
@@ -628,9 +709,10 @@ struct P3M {
       for (int s = 0; s < 14; ++s) {
         int cn = nb[s];
         if (cn < 0) continue;
-        int ipos = 0;
-        for (int i = cm.hoc[c]; i >= 0; i = cm.next[i], ++ipos) {
-          if (pairStride > 1 && ipos % pairStride) continue;
+        for (int i = cm.hoc[c]; i >= 0; i = cm.next[i]) {
+          // timing samples: every pairStride-th particle by index (unrelated to its place in
+          // the y-sorted list, whose early break makes low-y particles cheaper)
+          if (pairStride > 1 && i % pairStride) continue;
           for (int j = cm.hoc[cn]; j >= 0; j = cm.next[j]) {
             if (q.y_sorting && x[j].y - x[i].y > re) break;
             if (i == j) continue;
@@ -649,10 +731,31 @@ struct P3M {
       sr[i] = {};
       for (auto& s : slot[i]) s = {};
     }
+    if (fast && q.y_sorting) {
+      cm.fillSorted(pm.x);
+      nextCell = 0;
+      std::vector<std::thread> ts;
+      for (int t = 0; t < std::max(1, nthreads); ++t) ts.emplace_back(&P3M::fastJob, this);
+      for (auto& t : ts) t.join();
+      return;
+    }
     auto t0 = std::chrono::steady_clock::now();
-    cm.fill(pm.x, q.y_sorting != 0);
+    if (fillStride > 1 && q.y_sorting) {
+      // timing sample: the reference's insertion sort on every fillStride-th particle (its
+      // cost is quadratic in the cell populations, so the time is scaled by fillStride^2); the
+      // complete lists for the pair pass come from the equivalent stable sort, untimed
+      std::vector<V3<T>> xs;
+      for (int i = 0; i < pm.N; i += fillStride) xs.push_back(pm.x[i]);
+      ChainMesh<T> sub(&q, T(pm.p.H), int(xs.size()));
+      sub.fill(xs, true);
+      fillSec += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() *
+                 double(fillStride) * double(fillStride);
+      cm.fillSorted(pm.x);
+    } else {
+      cm.fill(pm.x, q.y_sorting != 0);
+      fillSec += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
     auto t1 = std::chrono::steady_clock::now();
-    fillSec += std::chrono::duration<double>(t1 - t0).count();
     int th = std::max(1, nthreads);
     std::vector<std::thread> ts;
     for (int t = 0; t < th; ++t) ts.emplace_back(&P3M::threadJob, this, t, th);
@@ -660,6 +763,7 @@ struct P3M {
     pairSec += std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
   }
   double fillSec = 0, pairSec = 0;
+  int fillStride = 1;  // timing samples: see shortRange()
   void correct() {  // correctAccelerations (p3mMethod.cpp:50-57)
     for (int i = 0; i < pm.N; ++i) {
       V3<T> tot{};
@@ -841,8 +945,9 @@ int pmAccel(const orc_pm_params* p, int n, const float* state, const float* mass
 template <typename T>
 int p3mAccel(const orc_pm_params* p, const orc_p3m_params* q, int n, const float* state,
              const float* masses, double* acc, double* acc_sr, int nthreads) {
-  PM<T> pm(p, n, state, masses, 1);
+  PM<T> pm(p, n, state, masses, nthreads);
   P3M<T> p3m(q, pm, nthreads);
+  p3m.fast = true;
   pm.toCode();
   pm.initGreen();
   pm.step();
@@ -906,12 +1011,14 @@ int port_p3m_run(int prec, const orc_pm_params* p, const orc_p3m_params* q, int 
   d.cap = diag ? diag_cap : 0;
   DiagOut* dp = diag ? &d : nullptr;
   if (prec) {
-    PM<double> pm(p, n, state, masses, 1);
+    PM<double> pm(p, n, state, masses, nthreads);
     P3M<double> p3m(q, pm, nthreads);
+    p3m.fast = true;
     runLoop<double>(pm, &p3m, sim_length, state_out, escaped, dp);
   } else {
-    PM<float> pm(p, n, state, masses, 1);
+    PM<float> pm(p, n, state, masses, nthreads);
     P3M<float> p3m(q, pm, nthreads);
+    p3m.fast = true;
     runLoop<float>(pm, &p3m, sim_length, state_out, escaped, dp);
   }
   if (diag_count) *diag_count = d.count;
@@ -1027,6 +1134,12 @@ int port_sr_table(const orc_p3m_params* q, float H, float* table, float* delta_s
 
 int port_time_steps(const orc_pm_params* p, const orc_p3m_params* q, int n, const float* state,
                     const float* masses, int steps, int nthreads, int pair_stride, double* out4) {
+  return port_time_steps2(p, q, n, state, masses, steps, nthreads, pair_stride, 1, out4, nullptr);
+}
+
+int port_time_steps2(const orc_pm_params* p, const orc_p3m_params* q, int n, const float* state,
+                     const float* masses, int steps, int nthreads, int pair_stride,
+                     int fill_stride, double* out4, double* wall) {
   // Times `steps` iterations of the run loop body (drift, force, kick) in float with nthreads
   // host threads.  With pair_stride S > 1 only every S-th particle of each cell list is an
   // i-particle of the pair pass (its j loops are complete), and the pair time is scaled by S.
@@ -1037,10 +1150,12 @@ int port_time_steps(const orc_pm_params* p, const orc_p3m_params* q, int n, cons
   if (q) {
     p3m = std::make_unique<P3M<float>>(q, pm, nthreads);
     p3m->pairStride = std::max(1, pair_stride);
+    p3m->fillStride = std::max(1, fill_stride);
   }
   pm.toCode();
   pm.initGreen();
   double pmSec = 0;
+  const auto w0 = std::chrono::steady_clock::now();
   for (int t = 0; t < steps; ++t) {
     for (int i = 0; i < n; ++i) pm.x[i] += pm.v[i];
     pm.statesToOriginal();
@@ -1054,6 +1169,7 @@ int port_time_steps(const orc_pm_params* p, const orc_p3m_params* q, int n, cons
     }
     for (int i = 0; i < n; ++i) pm.v[i] += pm.a[i];
   }
+  if (wall) *wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count();
   const int k = std::max(1, steps);
   const double fill = p3m ? p3m->fillSec / k : 0.0, pair = p3m ? p3m->pairSec / k : 0.0;
   out4[1] = pmSec / k;

@@ -34,6 +34,7 @@ EXPORTS = [
     "pmgb_tc_wait_probe",
     "pmgb_ensemble_create", "pmgb_ensemble_destroy", "pmgb_ensemble_run", "pmgb_ensemble_advance",
     "pmgb_ensemble_get_particles", "pmgb_ensemble_tuning", "pmgb_ensemble_size",
+    "pmgb_pm_get_stream", "pmgb_direct_sum_fp64",
     "pmgb_last_error", "pmgb_version",
 ]
 
@@ -137,6 +138,10 @@ def lib() -> C.CDLL:
         L.pmgb_ensemble_get_particles.argtypes = [vp, C.c_int, fp, fp, fp, C.c_int]
         L.pmgb_ensemble_tuning.argtypes = [vp, ip, ip, fp]
         L.pmgb_ensemble_size.argtypes = [vp, ip, C.POINTER(C.c_longlong)]
+        L.pmgb_pm_get_stream.argtypes = [vp, C.POINTER(vp)]
+        dp = C.POINTER(C.c_double)
+        L.pmgb_direct_sum_fp64.argtypes = [C.c_int, fp, fp, C.c_double, C.c_double, C.c_int, ip,
+                                           C.c_double, dp]
         L.pmgb_last_error.restype = C.c_char_p
         L.pmgb_version.restype = C.c_char_p
         _lib = L

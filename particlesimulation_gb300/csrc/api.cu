@@ -572,6 +572,12 @@ int pmgb_pm_size(pmgb_pm* h, int* n, int* grid3) {
   return PMGB_OK;
 }
 
+int pmgb_pm_get_stream(pmgb_pm* h, void** stream) {
+  if (!h || !stream) return set_error("null argument"), PMGB_EINVAL;
+  *stream = (void*)h->st;
+  return PMGB_OK;
+}
+
 // ------------------------------------------------------------------------- P3M -------
 int pmgb_p3m_create(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out) {
   if (!pm || !cfg || !out) return set_error("null argument"), PMGB_EINVAL;

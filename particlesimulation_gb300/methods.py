@@ -237,6 +237,12 @@ class PMMethod:
         check(lib().pmgb_pm_stage_times(self._h, _fp(t)))
         return dict(zip(["sort", "deposit", "poisson", "interpolation", "pair"], t.tolist()))
 
+    def stream(self) -> int:
+        """The handle's CUDA stream (cudaStream_t as an integer)."""
+        s = C.c_void_p()
+        check(lib().pmgb_pm_get_stream(self._h, C.byref(s)))
+        return int(s.value or 0)
+
 
 class PlummerSampler:
     """PlummerSampler(seed) (reference include/plummerSampler.h): ``sample(center, a, rMax, M,
@@ -315,6 +321,19 @@ class StateRecorder:
             self.close()
         except Exception:
             pass
+
+
+def direct_sum_fp64(pos, masses, G, idx, eps=0.0, periodic_L=0.0):
+    """FP64 direct-sum accelerations of the targets ``idx`` on the GPU (ppMethod's force,
+    reference source/ppMethod.cpp:23-36): (len(idx), 3) float64, same units as the inputs."""
+    pos = _f32(pos, (-1, 3))
+    m = _f32(masses).reshape(-1)
+    idx = np.ascontiguousarray(idx, np.int32).reshape(-1)
+    acc = np.zeros((len(idx), 3), np.float64)
+    check(lib().pmgb_direct_sum_fp64(len(m), _fp(pos), _fp(m), float(G), float(eps), len(idx),
+                                     idx.ctypes.data_as(C.POINTER(C.c_int)), float(periodic_L),
+                                     acc.ctypes.data_as(C.POINTER(C.c_double))))
+    return acc
 
 
 def fp32_peak_tflops() -> float:
