@@ -49,3 +49,14 @@ def rel_rms(a, b):
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
     return float(np.sqrt(((a - b) ** 2).sum(-1).mean() / (b ** 2).sum(-1).mean()))
+
+
+def err_stats(a, b):
+    """Per-particle relative force errors |a - b| / |b|: median and max, next to the
+    RMS-normalised figure of rel_rms."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    d = np.linalg.norm(a - b, axis=-1)
+    r = np.linalg.norm(b, axis=-1)
+    e = d / np.maximum(r, 1e-300)
+    return {"rms": rel_rms(a, b), "median": float(np.median(e)), "max": float(e.max())}

@@ -1,0 +1,153 @@
+"""The benchmark configurations at their stated sizes, on the GPU, against the FP64 oracle.
+
+  plummer_cluster   16,384-particle Plummer sphere, 64^3, CIC, 100 steps: the whole run against
+                    the oracle port's FP64 run (positions and velocities).
+  disk_p3m          262,144-particle disk + bulge P3M, 128^3, TSC, S2, cutoff 3 cells: 20 run
+                    iterations, repeated bit for bit, forces at the final state against the FP64
+                    oracle on sampled particles (the FP64 P3M run of the whole system costs about
+                    a minute per step on the CPU, so the run itself is checked through its
+                    final state).
+  blobs_periodic    4,194,304 particles, periodic 256^3, CIC: forces at t = 0 and after 10 steps
+                    on 4,096 sampled particles against the FP64 PM of all particles.
+  plummer_ensemble  64 systems x 100 steps in one launch per stage: every system equal to its
+                    single-system run.
+  disk_p3m_1m       1,048,576-particle disk P3M: 10 iterations, repeated bit for bit, forces at the
+                    final state against the FP64 oracle on sampled particles.
+
+Force errors are reported as per-particle relative errors (median, max) next to the RMS-normalised
+figure; the bars are stated per test (1e-5 for the FP32 path against FP64, the oracle port's own
+FP32 result sits at ~1-3e-6 on these workloads).
+"""
+import numpy as np
+import pytest
+
+from conftest import err_stats
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _cfg(w):
+    return O.PMConfig(grid=w.grid, box=w.box, H=w.H, DT=w.DT, G=w.G, interpolation=w.interpolation,
+                      finite_diff=w.finite_diff, greens=w.greens, diameter=w.diameter,
+                      periodic=int(w.periodic))
+
+
+def _q(w):
+    q = w.p3m
+    return O.P3MConfig(comp_box=q["comp_box"], cutoff=q["cutoff"], diameter=q["diameter"],
+                       softening=q["softening"], cloud_shape=q["cloud_shape"], use_table=q["table"],
+                       y_sorting=q["ysort"])
+
+
+def _pm(w):
+    import particlesimulation_gb300 as P
+    return P.PMMethod(w.state, w.mass, w.box, None, w.H, w.DT, w.G,
+                      P.InterpolationScheme(w.interpolation), P.FiniteDiffScheme(w.finite_diff),
+                      P.GreensFunction(w.greens), w.diameter, w.grid, periodic=w.periodic)
+
+
+def _p3m(pm, w):
+    import particlesimulation_gb300 as P
+    q = w.p3m
+    return P.P3MMethod(pm, q["comp_box"], q["cutoff"], q["diameter"], w.H, q["softening"],
+                       P.CloudShape(q["cloud_shape"]), bool(q["table"]), bool(q["ysort"]))
+
+
+def test_plummer_cluster_100_steps_vs_fp64_run(gpu_lib):
+    from particlesimulation_gb300 import workloads as W
+    w = W.plummer_cluster()
+    pm = _pm(w)
+    escaped, steps = pm.run(w.steps)
+    assert not escaped and steps == w.steps + 1
+    x, v, _ = pm.getParticles(units="original")
+    pm.close()
+    x64, v64, esc64 = O.port_run(_cfg(w), None, w.pos, w.vel, w.mass, w.steps, prec=1)
+    assert not esc64
+    # the oracle port in FP32 ends 2.1e-6 (positions, of the largest coordinate) and 1.2e-6
+    # (velocities, RMS) away from its FP64 run
+    assert np.abs(x - x64).max() < 1e-5 * np.abs(x64).max()
+    assert err_stats(v, v64)["rms"] < 1e-5
+
+
+def _run_twice(w, iters):
+    out = []
+    for _ in range(2):
+        pm = _pm(w)
+        p3m = _p3m(pm, w)
+        escaped, steps = p3m.run(iters - 1)
+        assert not escaped and steps == iters
+        x, v, _ = pm.getParticles(units="original")
+        out.append((pm, p3m, x.copy(), v.copy()))
+    (pm, p3m, x1, v1), (pm2, p3m2, x2, v2) = out
+    np.testing.assert_array_equal(x1, x2)  # deterministic pair pass and deposit
+    np.testing.assert_array_equal(v1, v2)
+    p3m2.close()
+    pm2.close()
+    return pm, p3m, x1, v1
+
+
+@pytest.mark.parametrize("name,iters,targets", [("disk_p3m", 20, 1500), ("disk_p3m_1m", 10, 1024)])
+def test_disk_p3m_run_state_at_size(gpu_lib, name, iters, targets):
+    from particlesimulation_gb300 import workloads as W
+    w = W.WORKLOADS[name]()
+    pm, p3m, x, v = _run_twice(w, iters)
+    assert np.isfinite(x).all() and np.isfinite(v).all()
+    # forces at the final state vs FP64 (PM of all particles + brute-force short range)
+    p3m.force()
+    x, _, acc = pm.getParticles(units="original")
+    acc = pm.getParticles(units="code")[2]
+    rng = np.random.default_rng(3)
+    idx = np.sort(rng.choice(w.n, targets, replace=False)).astype(np.int32)
+    f64 = O.port_p3m_accel_targets(_cfg(w), _q(w), x, np.zeros_like(x), w.mass, idx, prec=1)
+    st = err_stats(acc[idx], f64)
+    assert st["rms"] < 1e-5 and st["median"] < 1e-5, st
+    p3m.close()
+    pm.close()
+
+
+def test_blobs_periodic_forces_at_size(gpu_lib):
+    from particlesimulation_gb300 import workloads as W
+    w = W.blobs_periodic()
+    pm = _pm(w)
+    rng = np.random.default_rng(4096)
+    idx = np.sort(rng.choice(w.n, 4096, replace=False)).astype(np.int32)
+    for k in range(2):
+        if k == 0:
+            pm.pmMethodStep()
+        else:
+            escaped, _ = pm.run(9)  # 10 iterations; positions wrap in the periodic box
+            assert not escaped
+            pm.pmMethodStep()
+        x, v, _ = pm.getParticles(units="original")
+        acc = pm.getParticles(units="code")[2]
+        f64 = O.port_pm_accel(_cfg(w), x, v, w.mass, prec=1)
+        st = err_stats(acc[idx], f64[idx])
+        # the oracle port's FP32 result: RMS 1.0e-6, median 2.5e-6 at t = 0
+        assert st["rms"] < 1e-5 and st["median"] < 1e-5, st
+    pm.close()
+
+
+def test_plummer_ensemble_64_systems_100_steps(gpu_lib):
+    import particlesimulation_gb300 as P
+    from particlesimulation_gb300 import methods
+    from particlesimulation_gb300 import workloads as W
+    ws = W.plummer_ensemble()
+    assert len(ws) == 64
+    ens = methods.Ensemble([W.as_system(w) for w in ws])
+    esc, _ = ens.run(ws[0].steps)
+    assert not any(esc)
+    worst = 0.0
+    for s, w in enumerate(ws):
+        pm = P.PMMethod(w.state, w.mass, w.box, None, w.H, w.DT, w.G,
+                        P.InterpolationScheme(w.interpolation), P.FiniteDiffScheme(w.finite_diff),
+                        P.GreensFunction(w.greens), w.diameter, w.grid)
+        e1, _ = pm.run(w.steps)
+        x1, v1, _ = pm.getParticles(units="original")
+        pm.close()
+        x, v, _ = ens.getParticles(s, units="original")
+        assert not e1
+        worst = max(worst, np.abs(x - x1).max() / np.abs(x1).max(),
+                    np.abs(v - v1).max() / np.abs(v1).max())
+    ens.close()
+    assert worst <= 1e-6  # per system, relative to its largest coordinate / velocity
