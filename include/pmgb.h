@@ -65,7 +65,9 @@ typedef struct pmgb_external_field {
  * H, DT, G, is, fds, gFunc, particleDiameter, grid) (include/pmMethod.h:14-26) with the grid
  * given by its point counts, as PMMethodGPU takes it (include_gpu/PMMethodGPU.h:14-27). */
 typedef struct pmgb_pm_config {
-  int grid[3];          /* gridPoints (x, y, z); powers of two, 8..512 */
+  int grid[3];          /* gridPoints (x, y, z), each in [4, 4096]; meshes whose sides are all
+                           powers of two in [8, 512] take the specialised Poisson solve, others a
+                           mixed-radix one (any factors, as the reference's FFT plug-ins) */
   float box[3];         /* effectiveBoxSize, original units */
   float H, DT, G;
   int interpolation;    /* PMGB_NGP / PMGB_CIC / PMGB_TSC */
@@ -163,6 +165,28 @@ int pmgb_pm_size(pmgb_pm* pm, int* n, int* grid3);
  * closure handles over it enqueues its work; for callers that time or order their own work
  * against it.  No reference counterpart (the reference's GPU path uses the default stream). */
 int pmgb_pm_get_stream(pmgb_pm* pm, void** stream);
+
+/* ---------------------------------------------------------------- stepper ----------- */
+/* The leapfrog free functions of source/leapfrog.cpp:5-24 (include/leapfrog.h:6-12), in the
+ * reference's float arithmetic: */
+#define PMGB_LEAPFROG_HALF_KICK 0    /* setHalfStepVelocities:    v += 0.5 dt a */
+#define PMGB_LEAPFROG_DRIFT 1        /* updatePositions:          x += dt v */
+#define PMGB_LEAPFROG_KICK 2         /* updateVelocities:         v += dt a */
+#define PMGB_LEAPFROG_INTEGER_STEP 3 /* setIntegerStepVelocities: u = v + 0.5 dt a */
+/* On host arrays of n xyz triplets (the reference's std::vector<Particle> argument), computed on
+ * the device: pos is written by DRIFT, vel by the kicks, int_vel by INTEGER_STEP; arrays an
+ * operation does not use may be NULL. */
+int pmgb_leapfrog(int op, int n, float* pos, float* vel, const float* acc, float* int_vel, float dt);
+/* On a PM handle's particles on the device, code units (the reference's run loop calls them with
+ * dt = 1 in code units), with the accelerations of the handle's last force evaluation;
+ * INTEGER_STEP keeps u in the handle (read with pmgb_pm_get_integer_step_velocities). */
+int pmgb_pm_leapfrog(pmgb_pm* pm, int op, float dt);
+/* Particle::integerStepVelocity (include/particle.h:10) of every particle (original order) as
+ * the last PMGB_LEAPFROG_INTEGER_STEP set it (zero before), `units`. */
+int pmgb_pm_get_integer_step_velocities(pmgb_pm* pm, float* vel, int units);
+/* PMMethod::totalExternalForceOrigUnits (source/pmMethod.cpp:158-162): sum over particles of
+ * m g(x) in original units (zero without an external field); summed in double on the device. */
+int pmgb_pm_total_external_force(pmgb_pm* pm, float* force3);
 
 /* ---------------------------------------------------------------- run diagnostics ---- */
 
@@ -361,6 +385,16 @@ int pmgb_tc_wait_probe(int arrive, int spins);
 int pmgb_chaining_mesh_fill_noalloc(const float* d_pos, int n, const pmgb_p3m_config* cfg,
                                     float H, int* d_order, int* d_counts, int* dims3,
                                     void* stream);
+
+/* ---------------------------------------------------------------- FFT plug-in ------- */
+/* FFTAdapter<float>::fft / ifft (include/FFTAdapter.h:6-15; FFTWAdapter, source/FFTWAdapter.cpp:
+ * 27-43; KissFFTAdapter, include/kissFFTAdapter.h:16-29): 3D complex-to-complex transform of
+ * nx*ny*nz complex values (interleaved re, im; x fastest, as the reference's Grid stores its
+ * meshes), any lengths in [1, 8192].  Forward unnormalised; inverse = 1/(nx*ny*nz) times the
+ * unnormalised inverse, as the reference's adapters scale.  in and out are host arrays of
+ * 2*nx*ny*nz floats and may be the same array.  Mixed radix (4, 2, 3, 5, 7, other primes) on the
+ * device. */
+int pmgb_fft3d(int nx, int ny, int nz, const float* in, float* out, int inverse);
 
 /* ---------------------------------------------------------------- direct sum -------- */
 /* ppMethod's pairwise gravitational acceleration (source/ppMethod.cpp:23-36) restated in FP64

@@ -11,10 +11,14 @@
 // of a host std::function.
 #pragma once
 
+#include <cmath>
+#include <complex>
 #include <cstdio>
+#include <functional>
 #include <iostream>
 #include <stdexcept>
 #include <string>
+#include <array>
 #include <tuple>
 #include <vector>
 
@@ -125,6 +129,7 @@ class StateRecorder {
 struct Particle {
   Vec3 position, velocity, acceleration;
   float mass{};
+  Vec3 integerStepVelocity;  // set by setIntegerStepVelocities (include/particle.h:10)
 };
 
 // sphRadDecrField(pos, center, R, M, G) (reference source/externalFields.cpp:4-15), or none.
@@ -150,6 +155,103 @@ inline void check(int rc) {
   throw std::runtime_error(pmgb_last_error());
 }
 
+// The reference's FFT plug-in interface (include/FFTAdapter.h:6-15) and a device
+// implementation of it: 3D complex-to-complex transforms of x-fastest meshes of any size; ifft
+// includes the 1/N scale (source/FFTWAdapter.cpp:34-43).  dims = (nz, ny, nx), the order the
+// reference passes to its adapters (source/demos.cpp:758).
+template <typename T>
+class FFTAdapter {
+ public:
+  virtual ~FFTAdapter() {}
+  virtual std::vector<std::complex<T>>& fft(std::vector<std::complex<T>>& in,
+                                            std::vector<std::complex<T>>& out) = 0;
+  virtual std::vector<std::complex<T>>& ifft(std::vector<std::complex<T>>& in,
+                                             std::vector<std::complex<T>>& out) = 0;
+};
+
+class CudaFFTAdapter : public FFTAdapter<float> {
+ public:
+  explicit CudaFFTAdapter(std::array<int, 3> dims) : dims(dims) {}
+  std::vector<std::complex<float>>& fft(std::vector<std::complex<float>>& in,
+                                        std::vector<std::complex<float>>& out) override {
+    return run(in, out, 0);
+  }
+  std::vector<std::complex<float>>& ifft(std::vector<std::complex<float>>& in,
+                                         std::vector<std::complex<float>>& out) override {
+    return run(in, out, 1);
+  }
+
+ private:
+  std::vector<std::complex<float>>& run(std::vector<std::complex<float>>& in,
+                                        std::vector<std::complex<float>>& out, int inverse) {
+    const size_t L = size_t(dims[0]) * dims[1] * dims[2];
+    if (in.size() != L) throw std::invalid_argument("input size differs from the adapter's dims");
+    out.resize(L);
+    check(pmgb_fft3d(dims[2], dims[1], dims[0], reinterpret_cast<const float*>(in.data()),
+                     reinterpret_cast<float*>(out.data()), inverse));
+    return out;
+  }
+  static void check(int rc) {
+    if (rc == PMGB_EINVAL) throw std::invalid_argument(pmgb_last_error());
+    if (rc != PMGB_OK) throw std::runtime_error(pmgb_last_error());
+  }
+  std::array<int, 3> dims;
+};
+
+// Read-only copy of a PM handle's meshes with the reference Grid's getters (include/grid.h:10-
+// 70): x-fastest layout, density and field reads unwrapped, potential reads wrapped.  The field
+// is not kept on the device (the interpolation differences the potential on the fly); getField
+// differences the potential the same way (source/pmMethod.cpp:352-382).
+class Grid {
+ public:
+  Grid(int nx, int ny, int nz, FiniteDiffScheme fds)
+      : gridPointsX(nx), gridPointsY(ny), gridPointsZ(nz), length(nx * ny * nz), fds(fds),
+        density(size_t(length)), potential(size_t(length)),
+        greenHalf(size_t(nx / 2 + 1) * ny * nz) {}
+  std::tuple<int, int, int> indexTripleFromFlat(int flatIndex) const {
+    return std::make_tuple(flatIndex % gridPointsX, (flatIndex / gridPointsX) % gridPointsY,
+                           flatIndex / (gridPointsX * gridPointsY));
+  }
+  int getLength() const { return length; }
+  std::tuple<int, int, int> getGridPoints() const {
+    return std::make_tuple(gridPointsX, gridPointsY, gridPointsZ);
+  }
+  float getDensity(int x, int y, int z) const { return density[size_t(getIndx(x, y, z))]; }
+  float getPotential(int i, int j, int k) const { return potential[size_t(getWrappedIndx(i, j, k))]; }
+  // G(k) as the reference stores it (not divided by the mesh size), symmetrised over k and -k
+  std::complex<float> getGreensFunction(int i, int j, int k) const {
+    const int nxh = gridPointsX / 2 + 1;
+    if (i >= nxh) {
+      i = gridPointsX - i;
+      j = (gridPointsY - j) % gridPointsY;
+      k = (gridPointsZ - k) % gridPointsZ;
+    }
+    return {greenHalf[(size_t(k) * gridPointsY + j) * nxh + i] * float(length), 0.0f};
+  }
+  Vec3 getField(int x, int y, int z) const {
+    auto phi = [&](int a, int b, int c) { return getPotential(a, b, c); };
+    if (fds == FiniteDiffScheme::TWO_POINT)
+      return {-0.5f * (phi(x + 1, y, z) - phi(x - 1, y, z)), -0.5f * (phi(x, y + 1, z) - phi(x, y - 1, z)),
+              -0.5f * (phi(x, y, z + 1) - phi(x, y, z - 1))};
+    const float c = -1.0f / 12;
+    return {c * (-phi(x + 2, y, z) + 8 * phi(x + 1, y, z) - 8 * phi(x - 1, y, z) + phi(x - 2, y, z)),
+            c * (-phi(x, y + 2, z) + 8 * phi(x, y + 1, z) - 8 * phi(x, y - 1, z) + phi(x, y - 2, z)),
+            c * (-phi(x, y, z + 2) + 8 * phi(x, y, z + 1) - 8 * phi(x, y, z - 1) + phi(x, y, z - 2))};
+  }
+
+ private:
+  friend class PMMethodGPU;
+  static int mod(int a, int b) { return (a % b + b) % b; }
+  int getWrappedIndx(int i, int j, int k) const {
+    return mod(i, gridPointsX) + mod(j, gridPointsY) * gridPointsX +
+           mod(k, gridPointsZ) * gridPointsX * gridPointsY;
+  }
+  int getIndx(int i, int j, int k) const { return i + j * gridPointsX + k * gridPointsX * gridPointsY; }
+  int gridPointsX, gridPointsY, gridPointsZ, length;
+  FiniteDiffScheme fds;
+  std::vector<float> density, potential, greenHalf;
+};
+
 class PMMethodGPU {
  public:
   PMMethodGPU(const std::vector<Vec3>& state, const std::vector<float>& masses,
@@ -158,7 +260,7 @@ class PMMethodGPU {
               const InterpolationScheme is, const FiniteDiffScheme fds,
               const GreensFunction gFunc, const float particleDiameter,
               std::tuple<int, int, int> gridPoints)
-      : N(int(masses.size())), H(H), DT(DT), G(G) {
+      : N(int(masses.size())), H(H), DT(DT), G(G), fds(fds), ext(externalField) {
     if (state.size() != 2 * masses.size())
       throw std::invalid_argument("state must hold N positions followed by N velocities");
     pmgb_pm_config c{};
@@ -290,6 +392,39 @@ class PMMethodGPU {
     if (diagCapacity < capacity) setDiagnostics(capacity);
   }
 
+  // PMMethod::getGrid (include/pmMethod.h:37): the meshes of the last force evaluation, copied
+  // from the device into a read-only Grid with the reference's getters.
+  Grid getGrid() {
+    int n = 0, g[3];
+    check(pmgb_pm_size(h, &n, g));
+    Grid grid(g[0], g[1], g[2], fds);
+    check(pmgb_pm_get_density(h, grid.density.data()));
+    check(pmgb_pm_get_potential(h, grid.potential.data()));
+    check(pmgb_pm_get_greens_function(h, grid.greenHalf.data()));
+    return grid;
+  }
+
+  // PMMethod::getExternalPotential (include/pmMethod.h:38): the potential of the external field
+  // at a position in original units (sphRadDecrFieldPotential, source/externalFields.cpp:17-28).
+  std::function<float(Vec3)> getExternalPotential() const {
+    const ExternalField f = ext;
+    return [f](Vec3 pos) -> float {
+      if (!f.enabled) return 0.0f;
+      const float dx = pos.x - f.center.x, dy = pos.y - f.center.y, dz = pos.z - f.center.z;
+      const float r = std::sqrt(dx * dx + dy * dy + dz * dz);
+      if (r > f.R) return -f.G * f.M / r;
+      const float u = r / f.R;
+      return f.G * f.M / f.R * (-2 + u * u * (2 - u));
+    };
+  }
+
+  // PMMethod::totalExternalForceOrigUnits (source/pmMethod.cpp:158-162), on the device.
+  Vec3 totalExternalForceOrigUnits() {
+    Vec3 f;
+    check(pmgb_pm_total_external_force(h, &f.x));
+    return f;
+  }
+
   pmgb_pm* handle() { return h; }
 
  private:
@@ -297,6 +432,8 @@ class PMMethodGPU {
   int diagCapacity = 0;
   int N;
   float H, DT, G;
+  FiniteDiffScheme fds = FiniteDiffScheme::TWO_POINT;
+  ExternalField ext;
   std::vector<Particle> particles;
 };
 
@@ -353,6 +490,91 @@ class P3MMethod {
  private:
   PMMethodGPU& pm;
   pmgb_p3m* h = nullptr;
+};
+
+// The leapfrog free functions (include/leapfrog.h:6-12, source/leapfrog.cpp:5-24) on the
+// reference's particle vectors, computed on the device in the reference's float arithmetic ...
+namespace detail {
+inline void leapfrog(int op, std::vector<Particle>& particles, float dt) {
+  const size_t n = particles.size();
+  std::vector<float> pos(3 * n), vel(3 * n), acc(3 * n), u(3 * n);
+  for (size_t i = 0; i < n; ++i) {
+    const Particle& p = particles[i];
+    float* q[3] = {&pos[3 * i], &vel[3 * i], &acc[3 * i]};
+    const Vec3* v[3] = {&p.position, &p.velocity, &p.acceleration};
+    for (int k = 0; k < 3; ++k) {
+      q[k][0] = v[k]->x;
+      q[k][1] = v[k]->y;
+      q[k][2] = v[k]->z;
+    }
+  }
+  check(pmgb_leapfrog(op, int(n), pos.data(), vel.data(), acc.data(), u.data(), dt));
+  for (size_t i = 0; i < n; ++i) {
+    Particle& p = particles[i];
+    if (op == PMGB_LEAPFROG_DRIFT) p.position = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+    else if (op == PMGB_LEAPFROG_INTEGER_STEP) p.integerStepVelocity = {u[3 * i], u[3 * i + 1], u[3 * i + 2]};
+    else p.velocity = {vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]};
+  }
+}
+}  // namespace detail
+
+inline void setHalfStepVelocities(std::vector<Particle>& particles, float dt = 1.0f) {
+  detail::leapfrog(PMGB_LEAPFROG_HALF_KICK, particles, dt);
+}
+inline void setIntegerStepVelocities(std::vector<Particle>& particles, float dt = 1.0f) {
+  detail::leapfrog(PMGB_LEAPFROG_INTEGER_STEP, particles, dt);
+}
+inline void updateVelocities(std::vector<Particle>& particles, float dt = 1.0f) {
+  detail::leapfrog(PMGB_LEAPFROG_KICK, particles, dt);
+}
+inline void updatePositions(std::vector<Particle>& particles, float dt = 1.0f) {
+  detail::leapfrog(PMGB_LEAPFROG_DRIFT, particles, dt);
+}
+
+// ... and on a PM handle's own particles on the device (code units, the accelerations of its
+// last force evaluation); getParticles() reflects them after copyParticlesDeviceToHost().
+inline void setHalfStepVelocities(PMMethodGPU& pm, float dt = 1.0f) {
+  check(pmgb_pm_leapfrog(pm.handle(), PMGB_LEAPFROG_HALF_KICK, dt));
+}
+inline void setIntegerStepVelocities(PMMethodGPU& pm, float dt = 1.0f) {
+  check(pmgb_pm_leapfrog(pm.handle(), PMGB_LEAPFROG_INTEGER_STEP, dt));
+}
+inline void updateVelocities(PMMethodGPU& pm, float dt = 1.0f) {
+  check(pmgb_pm_leapfrog(pm.handle(), PMGB_LEAPFROG_KICK, dt));
+}
+inline void updatePositions(PMMethodGPU& pm, float dt = 1.0f) {
+  check(pmgb_pm_leapfrog(pm.handle(), PMGB_LEAPFROG_DRIFT, dt));
+}
+
+// AbstractStepper (include/abstractStepper.h:4-9) and a leapfrog stepper over a PM method: one
+// kick-drift-kick step of the particles in code units, the force from the PM (or P3M, when a
+// P3MMethod is attached to it) on the device.
+template <typename T>
+class AbstractStepper {
+ public:
+  virtual ~AbstractStepper() {}
+  virtual void doStep(std::vector<T>& x, float dt) = 0;
+};
+
+class LeapfrogStepper : public AbstractStepper<Particle> {
+ public:
+  explicit LeapfrogStepper(PMMethodGPU& pm) : pm(pm) {}
+  void doStep(std::vector<Particle>& x, float dt) override {
+    std::vector<Particle>& own = pm.getParticles();
+    if (x.size() != own.size()) throw std::invalid_argument("particle count differs from the PM method's");
+    own = x;
+    pm.copyParticlesHostToDevice();
+    pm.pmMethodStep();        // accelerations at x
+    setHalfStepVelocities(pm, dt);
+    updatePositions(pm, dt);
+    pm.pmMethodStep();        // accelerations at the new positions
+    setHalfStepVelocities(pm, dt);
+    pm.copyParticlesDeviceToHost();
+    x = own;
+  }
+
+ private:
+  PMMethodGPU& pm;
 };
 
 }  // namespace pmgb

@@ -34,7 +34,9 @@ EXPORTS = [
     "pmgb_tc_wait_probe",
     "pmgb_ensemble_create", "pmgb_ensemble_destroy", "pmgb_ensemble_run", "pmgb_ensemble_advance",
     "pmgb_ensemble_get_particles", "pmgb_ensemble_tuning", "pmgb_ensemble_size",
-    "pmgb_pm_get_stream", "pmgb_direct_sum_fp64",
+    "pmgb_pm_get_stream", "pmgb_direct_sum_fp64", "pmgb_fft3d",
+    "pmgb_leapfrog", "pmgb_pm_leapfrog", "pmgb_pm_get_integer_step_velocities",
+    "pmgb_pm_total_external_force",
     "pmgb_last_error", "pmgb_version",
 ]
 
@@ -142,6 +144,11 @@ def lib() -> C.CDLL:
         dp = C.POINTER(C.c_double)
         L.pmgb_direct_sum_fp64.argtypes = [C.c_int, fp, fp, C.c_double, C.c_double, C.c_int, ip,
                                            C.c_double, dp]
+        L.pmgb_fft3d.argtypes = [C.c_int, C.c_int, C.c_int, fp, fp, C.c_int]
+        L.pmgb_leapfrog.argtypes = [C.c_int, C.c_int, fp, fp, fp, fp, C.c_float]
+        L.pmgb_pm_leapfrog.argtypes = [vp, C.c_int, C.c_float]
+        L.pmgb_pm_get_integer_step_velocities.argtypes = [vp, fp, C.c_int]
+        L.pmgb_pm_total_external_force.argtypes = [vp, fp]
         L.pmgb_last_error.restype = C.c_char_p
         L.pmgb_version.restype = C.c_char_p
         _lib = L

@@ -36,6 +36,11 @@ static int ilog2(int v) {
 }
 static bool pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
 
+float mass_code_factor(float H, float DT, float G) {
+  volatile float c = DT * DT * 4 * std::numbers::pi_v<float> * G / (H * H * H);
+  return c;
+}
+
 }  // namespace pmgb
 
 using namespace pmgb;
@@ -62,22 +67,21 @@ void free_pm(pmgb_pm* h) {
     if (p) cudaFree(p);
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
+  if (h->gplans) gfft_plans_destroy(h->gplans);
+  if (h->ivel) cudaFree(h->ivel);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
 }
 
 // float arithmetic of include/unitConversions.h (reference), evaluated on the host
-inline float f_mass_to_code(float m, float H, float DT, float G) {
-  volatile float c = DT * DT * 4 * std::numbers::pi_v<float> * G / (H * H * H);
-  return c * m;
-}
+inline float f_mass_to_code(float m, float H, float DT, float G) { return mass_code_factor(H, DT, G) * m; }
 
 int check_cfg(const pmgb_pm_config* c, int n) {
   if (!c) return set_error("null config"), PMGB_EINVAL;
   if (n < 0) return set_error("negative particle count"), PMGB_EINVAL;
   for (int i = 0; i < 3; ++i)
-    if (!pow2(c->grid[i]) || c->grid[i] < 8 || c->grid[i] > 512)
-      return set_error("grid points must be powers of two in [8, 512]"), PMGB_EINVAL;
+    if (c->grid[i] < 4 || c->grid[i] > 4096)
+      return set_error("grid points must be in [4, 4096]"), PMGB_EINVAL;
   if (c->interpolation < 0 || c->interpolation > 2)
     return set_error("Unkown interpolation scheme"), PMGB_EINVAL;
   if (c->finite_diff < 0 || c->finite_diff > 1)
@@ -163,8 +167,12 @@ int force(pmgb_pm* h, int kdk, float kick, int drift, int tag, bool timed) {
   rc = launch_deposit(h->cfg.interpolation, h->pm[h->cur], n, h->m, h->sp.fx_scale, h->rho, stop, h->st);
   if (rc) return rc;
   if (timed) cudaEventRecord(h->ev[2], h->st);
-  rc = launch_poisson(h->rho, h->spec, h->phi, h->ghat, h->tw, h->nmax, h->m, h->sp.fx_inv, stop, h->st,
-                      diag_density(h));
+  if (h->generic)
+    rc = launch_poisson_generic(h->rho, h->spec, h->phi, h->ghat, h->gplans, h->m, h->sp.fx_inv, stop,
+                                h->st, diag_density(h));
+  else
+    rc = launch_poisson(h->rho, h->spec, h->phi, h->ghat, h->tw, h->nmax, h->m, h->sp.fx_inv, stop, h->st,
+                        diag_density(h));
   if (rc) return rc;
   if (timed) cudaEventRecord(h->ev[3], h->st);
   StepParams sp = h->sp;
@@ -320,23 +328,33 @@ int pmgb_pm_create(const pmgb_pm_config* cfg, int n, const float* state, const f
     if (cudaEventCreate(&e) != cudaSuccess) return set_error("cudaEventCreate failed"), fail(PMGB_ECUDA);
   const size_t N = std::max(n, 1);
   const size_t half = (size_t)m.nxp * m.ny * m.nz;
+  // powers of two in [8, 512] take the specialised half-spectrum Poisson solve (fft.cu); other
+  // meshes the mixed-radix one over a full complex mesh (gfft.cu)
+  for (int i = 0; i < 3; ++i)
+    if (!pow2(cfg->grid[i]) || cfg->grid[i] < 8 || cfg->grid[i] > 512) h->generic = true;
+  const size_t spec_elems = h->generic ? std::max(half, (size_t)m.L) : half;
   if ((rc = dalloc(&h->pm[0], N)) || (rc = dalloc(&h->pm[1], N)) || (rc = dalloc(&h->vi[0], N)) ||
       (rc = dalloc(&h->vi[1], N)) || (rc = dalloc(&h->acc, N)) || (rc = dalloc(&h->acc_pm, N)) ||
       (rc = dalloc(&h->keys, N)) || (rc = dalloc(&h->keys_alt, N)) || (rc = dalloc(&h->vals, N)) ||
       (rc = dalloc(&h->vals_alt, N)) || (rc = dalloc(&h->hist, radix_hist_words((int)N))) ||
-      (rc = dalloc(&h->rho, (size_t)m.L)) || (rc = dalloc(&h->spec, half)) || (rc = dalloc(&h->phi, (size_t)m.L)) ||
+      (rc = dalloc(&h->rho, (size_t)m.L)) || (rc = dalloc(&h->spec, spec_elems)) || (rc = dalloc(&h->phi, (size_t)m.L)) ||
       (rc = dalloc(&h->ghat, half)) || (rc = dalloc(&h->tw, (size_t)h->nmax / 2 + 1)) || (rc = dalloc(&h->flags, 4)) ||
       (rc = dalloc(&h->stage, 9 * N)) || (rc = dalloc(&h->mass_code, N)))
     return fail(rc);
   if (cudaMemsetAsync(h->rho, 0, (size_t)m.L * sizeof(u64), h->st) != cudaSuccess ||
-      cudaMemsetAsync(h->spec, 0, half * sizeof(float2), h->st) != cudaSuccess ||
+      cudaMemsetAsync(h->spec, 0, spec_elems * sizeof(float2), h->st) != cudaSuccess ||
       cudaMemsetAsync(h->phi, 0, (size_t)m.L * sizeof(float), h->st) != cudaSuccess ||
       cudaMemsetAsync(h->acc, 0, N * sizeof(float4), h->st) != cudaSuccess ||
       cudaMemsetAsync(h->flags, 0, 4 * sizeof(int), h->st) != cudaSuccess) {
     set_error("cudaMemset failed");
     return fail(PMGB_ECUDA);
   }
-  rc = fft_configure(m);
+  if (h->generic) {
+    const int dims[3] = {m.nx, m.ny, m.nz};
+    rc = gfft_plans_create(dims, &h->gplans);
+  } else {
+    rc = fft_configure(m);
+  }
   if (rc) return fail(rc);
   {
     std::vector<float2> tw(h->nmax / 2 + 1);

@@ -117,8 +117,8 @@ __global__ void green_kernel(float* __restrict__ ghat, MeshDims m, int gf, int i
       continue;
     }
     const double g1 = d_green(gf, is, fds, cs, a, kx, ky, kz, m);
-    const double g2 = d_green(gf, is, fds, cs, a, (m.nx - kx) & (m.nx - 1), (m.ny - ky) & (m.ny - 1),
-                              (m.nz - kz) & (m.nz - 1), m);
+    const double g2 = d_green(gf, is, fds, cs, a, (m.nx - kx) % m.nx, (m.ny - ky) % m.ny,
+                              (m.nz - kz) % m.nz, m);
     ghat[idx] = (float)(0.5 * (g1 + g2) * invL);
   }
 }

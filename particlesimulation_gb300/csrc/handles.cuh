@@ -29,6 +29,16 @@ int launch_poisson(u64* rho, float2* spec, float* phi, const float* ghat, const 
                    int nmax, MeshDims m, float fx_inv, const int* stop, cudaStream_t st,
                    float* rho_copy = nullptr);
 int launch_green(float* ghat, MeshDims m, int gf, int is, int fds, double a, cudaStream_t st);
+// m_code / m_orig in the float arithmetic of the reference's massToCodeUnits (api.cu)
+float mass_code_factor(float H, float DT, float G);
+// Mixed-radix Poisson solve for meshes whose sides are not powers of two in [8, 512] (gfft.cu):
+// plans (twiddle tables per axis) made once per handle; data = a full complex mesh.
+bool gfft_supported(int n);
+int gfft_plans_create(const int dims[3], void** out);
+void gfft_plans_destroy(void* plans);
+int launch_poisson_generic(u64* rho, float2* data, float* phi, const float* ghat, void* plans,
+                           MeshDims m, float fx_inv, const int* stop, cudaStream_t st,
+                           float* rho_copy);
 int launch_interp(bool kdk, float4* pm, float4* vi, float4* acc, int n, const float* phi,
                   const StepParams& sp, float kick, int drift, int* stop, cudaStream_t st);
 int launch_kick_drift(float4* pm, float4* vi, const float4* acc, int n, const StepParams& sp,
@@ -89,6 +99,9 @@ struct pmgb_pm {
   int equal_mass = 0;          // every particle has the same mass (pair pass folds it)
   pmgb_recorder* rec = nullptr;  // recorder of the current pmgb_pm_run_recorded, else null
   int rec_field = 0;
+  float4* ivel = nullptr;  // integer-step velocities, original order (pmgb_pm_leapfrog), lazily
+  bool generic = false;    // mesh not all powers of two in [8, 512]: mixed-radix Poisson solve
+  void* gplans = nullptr;  // its plans (gfft.cu)
 };
 
 struct pmgb_p3m {

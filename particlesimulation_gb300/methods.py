@@ -213,6 +213,19 @@ class PMMethod:
         check(lib().pmgb_pm_escaped(self._h, C.byref(e)))
         return bool(e.value)
 
+    def totalExternalForceOrigUnits(self):
+        """PMMethod::totalExternalForceOrigUnits (reference source/pmMethod.cpp:158-162)."""
+        f = np.zeros(3, np.float32)
+        check(lib().pmgb_pm_total_external_force(self._h, _fp(f)))
+        return f
+
+    def getIntegerStepVelocities(self, units: str = "code"):
+        """Particle::integerStepVelocity as the last setIntegerStepVelocities(pm) set it."""
+        u = np.zeros((self.N, 3), np.float32)
+        check(lib().pmgb_pm_get_integer_step_velocities(
+            self._h, _fp(u), UNITS_ORIGINAL if units == "original" else UNITS_CODE))
+        return u
+
     def getGridDensity(self):
         nx, ny, nz = self.gridPoints
         d = np.zeros(nx * ny * nz, np.float32)
@@ -321,6 +334,72 @@ class StateRecorder:
             self.close()
         except Exception:
             pass
+
+
+class FFTAdapter:
+    """FFTAdapter<float> (reference include/FFTAdapter.h:6-15): 3D complex-to-complex FFT of
+    complex64 arrays shaped (nz, ny, nx) (x fastest, the reference's mesh layout), any lengths;
+    ``ifft`` is scaled by 1/N like the reference's adapters (source/FFTWAdapter.cpp:34-43).
+    ``dims`` is (nz, ny, nx), as the reference passes it to FFTWAdapter / KissFFTAdapter
+    (source/demos.cpp:758)."""
+
+    def __init__(self, dims):
+        self.dims = tuple(int(d) for d in dims)
+
+    def _run(self, a, inverse, out=None):
+        nz, ny, nx = self.dims
+        a = np.ascontiguousarray(a, np.complex64).reshape(nz, ny, nx)
+        res = np.empty_like(a) if out is None else out
+        check(lib().pmgb_fft3d(nx, ny, nz, a.view(np.float32).ctypes.data_as(C.POINTER(C.c_float)),
+                               res.view(np.float32).ctypes.data_as(C.POINTER(C.c_float)),
+                               1 if inverse else 0))
+        return res
+
+    def fft(self, a, out=None):
+        return self._run(a, False, out)
+
+    def ifft(self, a, out=None):
+        return self._run(a, True, out)
+
+
+LEAPFROG_HALF_KICK, LEAPFROG_DRIFT, LEAPFROG_KICK, LEAPFROG_INTEGER_STEP = range(4)
+
+
+def _leapfrog(op, target, dt):
+    """A leapfrog operation on a PMMethod's device particles, or on a dict of (N, 3) float32
+    arrays {'position', 'velocity', 'acceleration', 'integerStepVelocity'} (updated in place)."""
+    if isinstance(target, PMMethod):
+        check(lib().pmgb_pm_leapfrog(target._h, op, C.c_float(dt)))
+        return target
+    arr = {k: _f32(target[k], (-1, 3)) for k in ("position", "velocity", "acceleration")}
+    n = len(arr["velocity"])
+    u = np.zeros((n, 3), np.float32)
+    check(lib().pmgb_leapfrog(op, n, _fp(arr["position"]), _fp(arr["velocity"]),
+                              _fp(arr["acceleration"]), _fp(u), C.c_float(dt)))
+    target.update(arr)
+    if op == LEAPFROG_INTEGER_STEP:
+        target["integerStepVelocity"] = u
+    return target
+
+
+def setHalfStepVelocities(particles, dt: float = 1.0):
+    """v += 0.5 dt a (reference source/leapfrog.cpp:5-8), on the device."""
+    return _leapfrog(LEAPFROG_HALF_KICK, particles, dt)
+
+
+def setIntegerStepVelocities(particles, dt: float = 1.0):
+    """u = v + 0.5 dt a (reference source/leapfrog.cpp:10-15), on the device."""
+    return _leapfrog(LEAPFROG_INTEGER_STEP, particles, dt)
+
+
+def updateVelocities(particles, dt: float = 1.0):
+    """v += dt a (reference source/leapfrog.cpp:17-20), on the device."""
+    return _leapfrog(LEAPFROG_KICK, particles, dt)
+
+
+def updatePositions(particles, dt: float = 1.0):
+    """x += dt v (reference source/leapfrog.cpp:22-24), on the device."""
+    return _leapfrog(LEAPFROG_DRIFT, particles, dt)
 
 
 def direct_sum_fp64(pos, masses, G, idx, eps=0.0, periodic_L=0.0):

@@ -2,7 +2,7 @@
 compiled from the reference sources by oracle/Makefile).
 
 Run where the reference sources exist:
-    python tests/golden/make_golden.py [diagnostics|recorder|samplers|field_sweeps]
+    python tests/golden/make_golden.py [diagnostics|recorder|samplers|field_sweeps|pm_accuracy]
 (with an argument, only that fixture is rewritten).
 Every case is a small seeded input; each fixture stores the inputs, the settings and the
 reference's outputs (float32), so tests on a machine without the reference still compare
@@ -257,6 +257,30 @@ def main():
     print("golden fixtures written to", HERE)
 
 
+def pm_accuracy_fixture():
+    """The reference's PM forces on the meshes of its accuracy scenario pmAccuracy
+    (source/demos.cpp:361-428): a linear disk from DiskSamplerLinear(42) (centre (30, 30, 15),
+    rb 3, mb 60, rd 15, md 15, thickness 0.3, G 4.5e-3; 2,000 particles here), effective box
+    60 x 60 x 30, meshes (2 Ng, 2 Ng, Ng) for Ng = 30, 34, 58 (not powers of two: factors 2, 3,
+    5, 17, 29), H = 60 / Ng, DT 1, discrete-Laplacian Green's function, every interpolation and
+    difference scheme at Ng = 30."""
+    n = 2000
+    st = O.ref_sample_disk_linear(42, np.array([30, 30, 15], np.float32), 3.0, 60.0, 15.0, 15.0,
+                                  0.3, 4.5e-3, n)
+    pos, vel = st[:n].astype(np.float32), st[n:].astype(np.float32)
+    mass = np.full(n, 15.0 / n, np.float32)
+    cases = {"inputs": dict(pos=pos, vel=vel, mass=mass)}
+    combos = [(30, is_, fds) for is_ in (0, 1, 2) for fds in (0, 1)] + [(34, 2, 0), (58, 1, 1)]
+    for ng, is_, fds in combos:
+        cfg = O.PMConfig(grid=(2 * ng, 2 * ng, ng), box=(60.0, 60.0, 30.0), H=60.0 / ng, DT=1.0,
+                         G=4.5e-3, interpolation=is_, finite_diff=fds, greens=0, diameter=0.0)
+        acc = O.ref_pm_accel(cfg, pos, vel, mass)
+        acc = acc[0] if isinstance(acc, tuple) else acc
+        cases[f"ng{ng}_is{is_}_fd{fds}"] = dict(acc=np.asarray(acc, np.float32), **_cfg_arrays(cfg))
+    np.savez_compressed(os.path.join(HERE, "pm_accuracy.npz"),
+                        **{f"{c}/{k}": a for c, dd in cases.items() for k, a in dd.items()})
+
+
 def _cfg_arrays(cfg):
     return dict(grid=np.array(cfg.grid, np.int32), box=np.array(cfg.box, np.float32),
                 HDTG=np.array([cfg.H, cfg.DT, cfg.G], np.float32),
@@ -280,9 +304,12 @@ if __name__ == "__main__":
         samplers_fixture()
     elif sys.argv[1:] == ["field_sweeps"]:
         field_sweeps_fixture()
+    elif sys.argv[1:] == ["pm_accuracy"]:
+        pm_accuracy_fixture()
     else:
         main()
         diagnostics_fixture()
         recorder_fixture()
         samplers_fixture()
         field_sweeps_fixture()
+        pm_accuracy_fixture()

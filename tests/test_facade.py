@@ -35,3 +35,8 @@ def test_facade_demo_runs(gpu_lib):
     acc0 = np.array([float(x) for x in lines["acc0"].split()])
     assert np.isfinite(acc0).all() and np.abs(acc0).max() > 0
     assert "invalid_argument" in out.stdout
+    g = lines["grid"].split()
+    assert g[:3] == ["32", "32", "32"] and float(g[3]) > 0
+    assert np.isfinite([float(x) for x in lines["step"].split()]).all()
+    assert float(lines["extforce"]) == 0.0 and float(lines["extpot"]) == 0.0  # no external field
+    assert float(lines["fftroundtrip"]) < 1e-5

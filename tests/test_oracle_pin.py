@@ -44,6 +44,22 @@ def test_port_pm_matches_golden(case):
     assert rel_rms(f64, d["acc"]) < 2e-5
 
 
+PMACC = load_npz("pm_accuracy.npz")
+
+
+@pytest.mark.parametrize("case", [c for c in PMACC if c != "inputs"])
+def test_port_pm_non_power_of_two_meshes_match_golden(case):
+    """Meshes of the reference's pmAccuracy scenario (2 Ng, 2 Ng, Ng) for Ng = 30, 34, 58: the
+    port's mixed-length FFT against the reference (kissfft) on the same inputs."""
+    d = PMACC[case]
+    inp = PMACC["inputs"]
+    cfg = cfg_from(d)
+    f32 = O.port_pm_accel(cfg, inp["pos"], inp["vel"], inp["mass"], prec=0)
+    f64 = O.port_pm_accel(cfg, inp["pos"], inp["vel"], inp["mass"], prec=1)
+    assert rel_rms(f32, d["acc"]) < 1e-5
+    assert rel_rms(f64, d["acc"]) < 1e-5
+
+
 @pytest.mark.parametrize("case", [c for c in PM if c != "inputs" and "density" in PM[c]])
 def test_port_pm_meshes_match_golden(case):
     d = PM[case]
