@@ -546,6 +546,24 @@ inline void updatePositions(PMMethodGPU& pm, float dt = 1.0f) {
   check(pmgb_pm_leapfrog(pm.handle(), PMGB_LEAPFROG_DRIFT, dt));
 }
 
+// Accelerations of every particle by the pairwise gravitational sum of ppMethod
+// (source/ppMethod.cpp:23-36), evaluated in FP64 on the device and rounded to float (the
+// reference sums in float); positions and result in the caller's units.
+inline std::vector<Vec3> ppAccelerations(const std::vector<Vec3>& positions, const std::vector<float>& masses,
+                                         float G, float softeningLength) {
+  const int n = int(masses.size());
+  if (positions.size() < masses.size()) throw std::invalid_argument("fewer positions than masses");
+  std::vector<int> idx(static_cast<size_t>(n));
+  for (int i = 0; i < n; ++i) idx[size_t(i)] = i;
+  std::vector<double> acc(3 * static_cast<size_t>(n));
+  check(pmgb_direct_sum_fp64(n, &positions[0].x, masses.data(), G, softeningLength, n, idx.data(), 0.0,
+                             acc.data()));
+  std::vector<Vec3> out(static_cast<size_t>(n));
+  for (int i = 0; i < n; ++i)
+    out[size_t(i)] = {float(acc[3 * size_t(i)]), float(acc[3 * size_t(i) + 1]), float(acc[3 * size_t(i) + 2])};
+  return out;
+}
+
 // AbstractStepper (include/abstractStepper.h:4-9) and a leapfrog stepper over a PM method: one
 // kick-drift-kick step of the particles in code units, the force from the PM (or P3M, when a
 // P3MMethod is attached to it) on the device.

@@ -138,8 +138,14 @@ __device__ __forceinline__ void fx_add_global(u64* p, long long v) {
 }
 
 __device__ __forceinline__ int wrapi(int a, int n) {
-  // n is a power of two, a may be negative (one stencil width outside)
-  return a & (n - 1);
+  // a mesh index wrapped into [0, n).  Powers of two: one AND, exact for any a.  Other sizes
+  // (the mixed-radix meshes): a is at most a stencil width outside the mesh for particles inside
+  // it; an index further out (a particle that left the box, whose run stops) is clamped so that
+  // every access stays inside the mesh.
+  if ((n & (n - 1)) == 0) return a & (n - 1);
+  a += a < 0 ? n : 0;
+  a -= a >= n ? n : 0;
+  return min(max(a, 0), n - 1);
 }
 
 // Exact product chain of the reference, with no contraction into FMA.

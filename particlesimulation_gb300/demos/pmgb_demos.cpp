@@ -8,11 +8,11 @@
 // Options: galaxy-sim-pm, galaxy-sim-p3m, galaxy-collision-sim-pm, galaxy-collision-sim-p3m,
 // cluster-sim-pm, cluster-sim-p3m, galaxy-sim-pm-timing, galaxy-sim-p3m-timing, and the PM field
 // sweeps anisotropy, finite-diff-err, assignment-schemes, poor-man-vs-laplacian, pm-optimal,
-// pm-optimal-var-diameter, pm-optimal-assignments.  Not provided: pm-accuracy-soft /
-// pm-accuracy-no-soft (meshes of 2 Ng x 2 Ng x Ng points for Ng = 30 .. 70, none a power of two,
-// which the transforms here require) and p3m-accuracy-assignments / p3m-accuracy-shapes (their
-// reference forces come from the direct-sum PP integrator, which is not part of this path); the
-// Barnes-Hut scenarios are out of scope as well.
+// pm-optimal-var-diameter, pm-optimal-assignments, and the accuracy scenarios pm-accuracy-soft,
+// pm-accuracy-no-soft, p3m-accuracy-assignments and p3m-accuracy-shapes.  Their direct-sum
+// reference forces (the reference's ppMethodLeapfrog with simLength 0: the accelerations of the
+// initial state and the positions after one drift) are computed in FP64 on the device and
+// rounded to float (the reference sums in float).  The Barnes-Hut scenarios are out of scope.
 // Differences from the reference's scenarios, all deliberate: the external field is passed as a
 // description (the GPU path has no host callbacks); galaxy-sim-p3m uses the reference's CPU
 // settings (S1-optimal influence function, a = 3H), which its CUDA build replaced by the
@@ -260,6 +260,129 @@ void pmOptimalAssignments(const std::string& out) {
   }
 }
 
+// One-frame StateRecorder file (int32 particle count, int32 frame count, float triplets;
+// source/stateRecorder.cpp:5-44, 109-119).
+void writeFrame(const std::string& out, const std::string& name, const std::vector<Vec3>& v) {
+  const std::string path = out + "/" + name;
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) throw std::runtime_error("cannot write " + path);
+  const int hdr[2] = {int(v.size()), 1};
+  std::fwrite(hdr, sizeof(int), 2, f);
+  std::fwrite(v.data(), sizeof(Vec3), v.size(), f);
+  std::fclose(f);
+}
+
+// ppMethodLeapfrog(state, masses, 0, DT = 1, G, eps, recorder, recordField = true)
+// (source/ppMethod.cpp:88-125): the field file holds the initial accelerations, the positions
+// file the positions after the first drift (half kick, then drift, dt = 1).
+void ppReference(const std::string& out, const std::vector<Vec3>& state, const std::vector<float>& masses,
+                 float G, float eps, const std::string& positionsFile, const std::string& forceFile) {
+  const size_t n = masses.size();
+  std::vector<Vec3> pos(state.begin(), state.begin() + long(n));
+  std::vector<Vec3> acc = ppAccelerations(pos, masses, G, eps);
+  std::vector<Particle> ps(n);
+  for (size_t i = 0; i < n; ++i) {
+    ps[i].position = pos[i];
+    ps[i].velocity = state[n + i];
+    ps[i].acceleration = acc[i];
+    ps[i].mass = masses[i];
+  }
+  setHalfStepVelocities(ps);
+  updatePositions(ps);
+  for (size_t i = 0; i < n; ++i) pos[i] = ps[i].position;
+  writeFrame(out, forceFile, acc);
+  writeFrame(out, positionsFile, pos);
+}
+
+// The disk of the accuracy scenarios (source/demos.cpp:361-373, 593-605)
+void accuracyDisk(std::vector<Vec3>& state, std::vector<float>& masses, float& G) {
+  const int n = 10000;
+  G = 4.5e-3f;
+  DiskSamplerLinear diskSampler(42);
+  state = diskSampler.sample(v3(30, 30, 15), 3.0f, 60.0f, 15.0f, 15.0f, 0.3f, G, n);
+  masses.assign(size_t(n), 15.0f / n);
+}
+
+const char* name(InterpolationScheme is) {
+  return is == InterpolationScheme::NGP ? "NGP" : is == InterpolationScheme::CIC ? "CIC" : "TSC";
+}
+// the reference's toString names in its file names (source/demos.cpp:63-96)
+const char* name(FiniteDiffScheme f) { return f == FiniteDiffScheme::TWO_POINT ? "2-point" : "4-point"; }
+const char* name(GreensFunction g) {
+  return g == GreensFunction::S1_OPTIMAL ? "S1" : g == GreensFunction::S2_OPTIMAL ? "S2" : "Unknown";
+}
+
+// pm-accuracy-soft / pm-accuracy-no-soft (pmAccuracy, source/demos.cpp:361-428): PM forces of
+// the disk on (2 Ng, 2 Ng, Ng) meshes, Ng = 30, 34, ..., 70, every interpolation and difference
+// scheme; direct-sum forces with softening box / Ng (soft) or one without (no-soft)
+void pmAccuracy(const std::string& out, bool ppSoftening) {
+  std::vector<Vec3> state;
+  std::vector<float> masses;
+  float G;
+  accuracyDisk(state, masses, G);
+  const int n = int(masses.size());
+  const auto box = std::make_tuple(60.0f, 60.0f, 30.0f);
+  const int NgStart = 30, NgEnd = 70, NgStep = 4;
+  if (ppSoftening) {
+    for (int Ng = NgStart; Ng <= NgEnd; Ng += NgStep)
+      ppReference(out, state, masses, G, std::get<0>(box) / Ng, "positions-pp.dat",
+                  "force-pp-" + std::to_string(Ng) + ".dat");
+  } else {
+    ppReference(out, state, masses, G, 0.0f, "positions-pp.dat", "force-pp-0.dat");
+  }
+  for (auto is : {InterpolationScheme::NGP, InterpolationScheme::CIC, InterpolationScheme::TSC})
+    for (auto fds : {FiniteDiffScheme::TWO_POINT, FiniteDiffScheme::FOUR_POINT})
+      for (int Ng = NgStart; Ng <= NgEnd; Ng += NgStep) {
+        const auto gridPoints = std::make_tuple(2 * Ng, 2 * Ng, Ng);
+        const float H = std::get<0>(box) / (std::get<0>(gridPoints) / 2);
+        const std::string forceFile =
+            std::string("force-pm-") + name(is) + "-" + name(fds) + "-" + std::to_string(Ng) + ".dat";
+        std::cout << forceFile << '\n';
+        StateRecorder stateRecorder(n, 1, out, "positions-pm.dat", "", "", "", "", forceFile.c_str());
+        PMMethodGPU pm(state, masses, box, ExternalField::none(), H, 1.0f, G, is, fds,
+                       GreensFunction::DISCRETE_LAPLACIAN, 0.0f, gridPoints);
+        pm.run(stateRecorder, 0, false, true);
+      }
+}
+
+// p3m-accuracy-assignments / p3m-accuracy-shapes (source/demos.cpp:593-727): P3M forces of the
+// disk on the 128 x 128 x 64 mesh for particle diameters a = 0.2 aMul H, aMul = 5 .. 25,
+// cutoff re = a, table-free short-range force, unsorted chaining mesh
+void p3mAccuracy(const std::string& out, bool shapes) {
+  std::vector<Vec3> state;
+  std::vector<float> masses;
+  float G;
+  accuracyDisk(state, masses, G);
+  const int n = int(masses.size());
+  const auto box = std::make_tuple(60.0f, 60.0f, 30.0f);
+  ppReference(out, state, masses, G, 0.0f, "positions-pp.dat", "force-pp.dat");
+  const auto gridPoints = std::make_tuple(128, 128, 64);
+  const float H = std::get<0>(box) / (std::get<0>(gridPoints) / 2);
+  auto one = [&](InterpolationScheme is, FiniteDiffScheme fds, GreensFunction gf, int aMul,
+                 const std::string& forceFile) {
+    const float a = 0.2f * aMul * H;
+    std::cout << forceFile << '\n';
+    StateRecorder stateRecorder(n, 1, out, "positions-pm.dat", "", "", "", "", forceFile.c_str());
+    PMMethodGPU pm(state, masses, box, ExternalField::none(), H, 1.0f, G, is, fds, gf, a, gridPoints);
+    P3MMethod p3m(pm, box, a, a, H, 0.0f,
+                  gf == GreensFunction::S2_OPTIMAL ? CloudShape::S2 : CloudShape::S1, false, false);
+    p3m.run(stateRecorder, 0, false, true);
+  };
+  if (!shapes) {
+    for (auto is : {InterpolationScheme::NGP, InterpolationScheme::CIC, InterpolationScheme::TSC})
+      for (auto fds : {FiniteDiffScheme::TWO_POINT, FiniteDiffScheme::FOUR_POINT})
+        for (int aMul = 5; aMul <= 25; ++aMul)
+          one(is, fds, GreensFunction::S1_OPTIMAL, aMul,
+              std::string("force-p3m-") + name(is) + "-" + name(fds) + "-" + std::to_string(aMul) + ".dat");
+  } else {
+    for (auto gf : {GreensFunction::S1_OPTIMAL, GreensFunction::S2_OPTIMAL})
+      for (auto fds : {FiniteDiffScheme::TWO_POINT, FiniteDiffScheme::FOUR_POINT})
+        for (int aMul = 5; aMul <= 25; ++aMul)
+          one(InterpolationScheme::TSC, fds, gf, aMul,
+              std::string("force-p3m-TSC-") + name(fds) + "-" + name(gf) + "-" + std::to_string(aMul) + ".dat");
+  }
+}
+
 }  // namespace
 
 int main(int argc, char* argv[]) {
@@ -284,6 +407,10 @@ int main(int argc, char* argv[]) {
         {"pm-optimal", [&] { pmOptimal(out); }},
         {"pm-optimal-var-diameter", [&] { pmOptimalVaryingDiameter(out); }},
         {"pm-optimal-assignments", [&] { pmOptimalAssignments(out); }},
+        {"pm-accuracy-soft", [&] { pmAccuracy(out, true); }},
+        {"pm-accuracy-no-soft", [&] { pmAccuracy(out, false); }},
+        {"p3m-accuracy-assignments", [&] { p3mAccuracy(out, false); }},
+        {"p3m-accuracy-shapes", [&] { p3mAccuracy(out, true); }},
         // galaxySimulationPMTiming / P3MTiming (source/demos.cpp:779-836, 953-1016): "n seconds"
         {"galaxy-sim-pm-timing",
          [&] {

@@ -83,3 +83,56 @@ def test_field_sweep_matches_reference(gpu_lib, option, files, case, tmp_path):
             for k in range(len(a)):
                 rel = np.sqrt(((a[k] - b[k]) ** 2).sum() / (b[k] ** 2).sum())
                 assert rel < 3e-5, (name, k, rel)
+
+
+@pytest.mark.parametrize("option,nfiles", [("pm-accuracy-no-soft", 2 + 66), ("p3m-accuracy-shapes", 2 + 84)])
+def test_accuracy_scenarios(gpu_lib, option, nfiles, tmp_path):
+    """The reference's accuracy scenarios (pmAccuracy on (2 Ng, 2 Ng, Ng) meshes, Ng = 30..70,
+    and p3mAccuracyShapes on 128 x 128 x 64 for a = 0.2 aMul H): the reference's file names,
+    one frame of 10,000 particles each; the direct-sum forces equal the FP64 oracle's at the
+    sampler's positions, and a PM / P3M force file equals the FP64 oracle's forces at the
+    positions it was computed at (positions-pm.dat), 1e-5 RMS-normalised."""
+    import particlesimulation_gb300 as P
+    from conftest import rel_rms
+    from oracle import oracle as O
+    from particlesimulation_gb300 import build
+    exe = build.build_demos()
+    r = subprocess.run([exe, option, str(tmp_path)], capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout + r.stderr
+    names = os.listdir(tmp_path)
+    assert len(names) == nfiles and "positions-pp.dat" in names and "positions-pm.dat" in names
+    n = 10000
+    state = P.DiskSamplerLinear(42).sample((30, 30, 15), 3.0, 60.0, 15.0, 15.0, 0.3, 4.5e-3, n)
+    mass = np.full(n, 15.0 / n, np.float32)
+    pp_name = "force-pp-0.dat" if option == "pm-accuracy-no-soft" else "force-pp.dat"
+    with open(tmp_path / pp_name, "rb") as f:
+        (h, a) = _frames(f.read())
+    assert h == (n, 1)
+    want = O.port_pp_accel(state[:n].astype(np.float64), mass.astype(np.float64), 4.5e-3)
+    assert rel_rms(a[0], want) < 1e-6
+    with open(tmp_path / "positions-pm.dat", "rb") as f:
+        (h, x) = _frames(f.read())
+    assert h == (n, 1)
+    if option == "pm-accuracy-no-soft":
+        fname, cfg, q = "force-pm-TSC-2-point-34.dat", O.PMConfig(
+            grid=(68, 68, 34), box=(60.0, 60.0, 30.0), H=60.0 / 34, DT=1.0, G=4.5e-3,
+            interpolation=2, finite_diff=0, greens=0, diameter=0.0), None
+    else:
+        H = 60.0 / 64
+        a_ = float(np.float32(0.2) * np.float32(25) * np.float32(H))
+        fname = "force-p3m-TSC-4-point-S2-25.dat"
+        cfg = O.PMConfig(grid=(128, 128, 64), box=(60.0, 60.0, 30.0), H=H, DT=1.0, G=4.5e-3,
+                         interpolation=2, finite_diff=1, greens=2, diameter=a_)
+        q = O.P3MConfig(comp_box=(60.0, 60.0, 30.0), cutoff=a_, diameter=a_, softening=0.0,
+                        cloud_shape=1, use_table=0, y_sorting=0)
+    with open(tmp_path / fname, "rb") as f:
+        (h, fa) = _frames(f.read())
+    assert h == (n, 1) and np.isfinite(fa).all()
+    xs = x[0].astype(np.float32)
+    if q is None:
+        ref = O.port_pm_accel(cfg, xs, np.zeros_like(xs), mass, prec=1)
+    else:
+        ref = O.port_p3m_accel(cfg, q, xs, np.zeros_like(xs), mass, prec=1)
+        ref = ref[0] if isinstance(ref, tuple) else ref
+    ref = np.asarray(ref) * (cfg.H / cfg.DT ** 2)  # code -> original units
+    assert rel_rms(fa[0], ref) < 1e-5, fname
