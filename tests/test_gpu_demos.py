@@ -85,7 +85,7 @@ def test_field_sweep_matches_reference(gpu_lib, option, files, case, tmp_path):
                 assert rel < 3e-5, (name, k, rel)
 
 
-@pytest.mark.parametrize("option,nfiles", [("pm-accuracy-no-soft", 2 + 66), ("p3m-accuracy-shapes", 2 + 84)])
+@pytest.mark.parametrize("option,nfiles", [("pm-accuracy-no-soft", 3 + 66), ("p3m-accuracy-shapes", 3 + 84)])
 def test_accuracy_scenarios(gpu_lib, option, nfiles, tmp_path):
     """The reference's accuracy scenarios (pmAccuracy on (2 Ng, 2 Ng, Ng) meshes, Ng = 30..70,
     and p3mAccuracyShapes on 128 x 128 x 64 for a = 0.2 aMul H): the reference's file names,
