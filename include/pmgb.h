@@ -378,10 +378,12 @@ int pmgb_tc_wait_probe(int arrive, int spins);
  * units (device memory), d_order = n ints, d_counts = Mx*My*Mz ints (device memory), dims3 =
  * (Mx, My, Mz) on the host; cfg supplies comp_box, cutoff and y_sorting.  Runs on `stream`
  * (a cudaStream_t, NULL = default stream) without synchronising.  Limits: n <= 262,144 and
- * Mx*My*Mz <= 262,142; larger inputs return PMGB_EINVAL.  Its scratch (about 6.5 MB) is a
- * fixed device array held on every GPU that loads the library; the first call on a device
- * looks its address up (call it once before any stream capture); calls that overlap on the
- * GPU share the scratch and race. */
+ * Mx*My*Mz <= 262,142; larger inputs return PMGB_EINVAL.  Its scratch (about 7.1 MiB) is a
+ * fixed device array; under lazy module loading it is loaded on the first call on each device
+ * (that call also looks its address up, so make it before any stream capture or any section
+ * that must not allocate) and held until exit; calls that overlap on the GPU share the scratch
+ * and race.  Particles outside the chaining mesh are not listed: d_order holds sum(counts)
+ * entries and the rest of it is left as it was. */
 int pmgb_chaining_mesh_fill_noalloc(const float* d_pos, int n, const pmgb_p3m_config* cfg,
                                     float H, int* d_order, int* d_counts, int* dims3,
                                     void* stream);

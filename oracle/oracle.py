@@ -103,9 +103,10 @@ def build_port() -> None:
 
 
 def build_ref() -> bool:
-    """Compile the reference CPU path from its sources; False where they are absent."""
-    ref = os.environ.get("PSIM_REFERENCE", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "source")):
+    """Compile the reference CPU path from its sources (the checkout named by the PSIM_REFERENCE
+    environment variable); False where it is not set or the sources are absent."""
+    ref = os.environ.get("PSIM_REFERENCE")
+    if not ref or not os.path.isdir(os.path.join(ref, "source")):
         return False
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFERENCE={ref}"], check=True)
     return True

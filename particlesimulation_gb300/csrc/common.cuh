@@ -33,6 +33,10 @@ void count_launches(int k);
     }                                                                              \
   } while (0)
 
+// Keys per block of the LSD radix sort (sort.cu): its histogram holds 256 words per block of
+// RS_TILE keys plus 256 row totals (radix_hist_words).
+constexpr int RS_TILE = 4096;
+
 // ---------------------------------------------------------------- parameters --------
 // Everything a kernel needs about one system, passed by value.
 struct MeshDims {

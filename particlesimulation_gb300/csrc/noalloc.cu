@@ -8,13 +8,17 @@
 // or descending index) from caller-owned device input and output buffers, using only scratch
 // that lives in file-scope __device__ arrays of fixed size:
 //
-//   at most kNoAllocMaxParticles = 262,144 particles and kNoAllocMaxCells = 262,144 cells;
-//   about 6.5 MB of device memory, held on every GPU that loads this library until exit.
+//   at most kNoAllocMaxParticles = 262,144 particles and kNoAllocMaxCells - 2 = 262,142 cells;
+//   about 7.1 MiB (7.4 MB) of device memory: sort keys 4 MiB, values 2 MiB, cell starts 1 MiB,
+//   radix histogram 66 KB.  Under CUDA's lazy module loading (the default) the module holding
+//   them, and so the scratch, is loaded on the first call on each device and then held until
+//   the process exits.
 //
 // Host code cannot use those arrays' names as device addresses (on the host they are stand-in
 // symbols), so on the first call on each device, with that device current, the device
-// addresses are looked up with cudaGetSymbolAddress; that first call should therefore come
-// before any CUDA graph capture.  All calls share the same arrays: calls that may overlap on the
+// addresses are looked up with cudaGetSymbolAddress.  That first call is where the module and
+// its scratch get loaded, so it should come before any CUDA graph capture and before any
+// section of the caller's that must not allocate.  All calls share the same arrays: calls that may overlap on the
 // GPU (different streams, or host threads calling concurrently) race and must be serialised by
 // the caller.  Every call overwrites all of the scratch it reads, so nothing from a previous
 // call leaks into the next.
@@ -26,7 +30,9 @@ namespace pmgb {
 
 constexpr int kNoAllocMaxParticles = 262144;
 constexpr int kNoAllocMaxCells = 262144;
-constexpr int kNoAllocHistBlocks = (kNoAllocMaxParticles + 4095) / 4096;  // radix tile = 4096 keys
+// radix_sort_pairs writes radix_hist_words(n) = 256 radix_hist_blocks(n) + 256 histogram words,
+// one block per RS_TILE keys (the constant the sort itself is built with)
+constexpr int kNoAllocHistBlocks = (kNoAllocMaxParticles + RS_TILE - 1) / RS_TILE;
 
 static __device__ __align__(256) u64 g_na_keys[2][kNoAllocMaxParticles];
 static __device__ __align__(256) u32 g_na_vals[2][kNoAllocMaxParticles];

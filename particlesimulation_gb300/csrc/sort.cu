@@ -20,7 +20,7 @@ namespace pmgb {
 constexpr int RS_THREADS = 256;
 constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int RS_STRIPS = 16;                          // 32-key strips per warp
-constexpr int RS_TILE = RS_WARPS * RS_STRIPS * 32;     // 4096 keys per block
+static_assert(RS_WARPS * RS_STRIPS * 32 == RS_TILE, "RS_TILE (common.cuh) is the keys per block");
 
 __device__ __forceinline__ u32 lanemask_lt() {
   u32 m;

@@ -1,8 +1,9 @@
 """Generates tests/golden/*.npz from the reference's own CPU code (oracle/_ref/libpsref.so,
 compiled from the reference sources by oracle/Makefile).
 
-Run where the reference sources exist:
-    python tests/golden/make_golden.py [diagnostics|recorder|samplers|field_sweeps|pm_accuracy]
+Run where the reference sources exist, naming the checkout:
+    PSIM_REFERENCE=<reference checkout> python tests/golden/make_golden.py \
+        [diagnostics|recorder|samplers|field_sweeps|pm_accuracy]
 (with an argument, only that fixture is rewritten).
 Every case is a small seeded input; each fixture stores the inputs, the settings and the
 reference's outputs (float32), so tests on a machine without the reference still compare
@@ -166,7 +167,7 @@ def samplers_fixture():
 
 
 def main():
-    assert O.build_ref(), "reference sources not found"
+    assert O.build_ref(), "set PSIM_REFERENCE to the reference checkout"
     os.makedirs(HERE, exist_ok=True)
     # ---- PM forces (single pmMethodStep after unit conversion and Green's function)
     p, v, m = inputs(10, 600, 3.0, 27.0)

@@ -90,8 +90,9 @@ def test_accuracy_scenarios(gpu_lib, option, nfiles, tmp_path):
     """The reference's accuracy scenarios (pmAccuracy on (2 Ng, 2 Ng, Ng) meshes, Ng = 30..70,
     and p3mAccuracyShapes on 128 x 128 x 64 for a = 0.2 aMul H): the reference's file names,
     one frame of 10,000 particles each; the direct-sum forces equal the FP64 oracle's at the
-    sampler's positions, and a PM / P3M force file equals the FP64 oracle's forces at the
-    positions it was computed at (positions-pm.dat), 1e-5 RMS-normalised."""
+    sampler's positions, and a PM / P3M force file (the accelerations a run records before its
+    first drift, source/pmMethod.cpp:79-85) equals the FP64 oracle's forces at the sampler's
+    positions, 1e-5 RMS-normalised."""
     import particlesimulation_gb300 as P
     from conftest import rel_rms
     from oracle import oracle as O
@@ -128,7 +129,7 @@ def test_accuracy_scenarios(gpu_lib, option, nfiles, tmp_path):
     with open(tmp_path / fname, "rb") as f:
         (h, fa) = _frames(f.read())
     assert h == (n, 1) and np.isfinite(fa).all()
-    xs = x[0].astype(np.float32)
+    xs = np.ascontiguousarray(state[:n], np.float32)
     if q is None:
         ref = O.port_pm_accel(cfg, xs, np.zeros_like(xs), mass, prec=1)
     else:

@@ -4,9 +4,10 @@ allocating one (a P3M handle's pmgb_p3m_get_cell_lists).
 It serves callers that cannot allocate device memory at the call site: hosts that hand this
 library buffers out of their own fixed pool, or step loops that must not call cudaMalloc.  The
 caller owns inputs and outputs (here allocated by torch, standing in for such a host); the
-entry point itself only uses its fixed scratch arrays.  Cell lists are integer data, so the
-comparison is exact, as for the other cell-list tests.  Two calls in a row with different
-inputs check that nothing from one call leaks into the next.  This file is collected last.
+entry point itself only uses its fixed scratch arrays: after the first call on a device the
+free device memory is unchanged across a call.  Cell lists are integer data, so the comparison
+is exact, as for the other cell-list tests.  Two calls in a row with different inputs check that
+nothing from one call leaks into the next.  This file is collected last.
 """
 import ctypes as C
 
@@ -33,7 +34,7 @@ def _allocating_cell_lists(pos_code, H, comp_box, cutoff, ysort):
     return out
 
 
-def _noalloc_cell_lists(lib, pos_code, H, comp_box, cutoff, ysort):
+def _noalloc_cell_lists(lib, pos_code, H, comp_box, cutoff, ysort, check_free=False):
     import torch
     from particlesimulation_gb300 import _lib
     cfg = _lib.P3MConfigC()
@@ -44,17 +45,20 @@ def _noalloc_cell_lists(lib, pos_code, H, comp_box, cutoff, ysort):
     cfg.use_table = 1
     cfg.y_sorting = ysort
     n = len(pos_code)
-    mx = int(np.float32(comp_box[0]) / np.float32(cutoff))
-    d_pos = torch.from_numpy(np.ascontiguousarray(pos_code, np.float32)).cuda()
-    d_order = torch.full((n,), -7, dtype=torch.int32, device="cuda")
-    d_counts = torch.full((mx ** 3,), -7, dtype=torch.int32, device="cuda")
+    ncells = int(np.prod([int(np.float32(b) / np.float32(cutoff)) for b in comp_box]))
+    d_pos = torch.from_numpy(np.ascontiguousarray(pos_code, np.float32).reshape(-1, 3)).cuda()
+    d_order = torch.full((max(n, 1),), -7, dtype=torch.int32, device="cuda")
+    d_counts = torch.full((ncells,), -7, dtype=torch.int32, device="cuda")
     dims = (C.c_int * 3)()
     torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
     rc = lib.pmgb_chaining_mesh_fill_noalloc(C.c_void_p(d_pos.data_ptr()), n, C.byref(cfg),
                                              C.c_float(H), C.c_void_p(d_order.data_ptr()),
                                              C.c_void_p(d_counts.data_ptr()), dims, None)
     assert rc == 0, lib.pmgb_last_error()
     torch.cuda.synchronize()
+    if check_free:  # after the first call on this device nothing more is allocated
+        assert torch.cuda.mem_get_info()[0] == free0
     counts = d_counts.cpu().numpy()
     return d_order.cpu().numpy()[: counts.sum()], counts, (dims[0], dims[1], dims[2])
 
@@ -71,12 +75,42 @@ def test_noalloc_cell_lists_match_allocating_entry_point(gpu_lib, ysort):
     inputs.append(a)
     b = np.clip(rng.normal(8, 2.5, (3000, 3)), 0, 15.99).astype(np.float32)
     inputs.append(b)
-    for pos in inputs:  # two calls in a row, different sizes and contents
+    for k, pos in enumerate(inputs):  # two calls in a row, different sizes and contents
         want = _allocating_cell_lists(pos, H, comp_box, cutoff, ysort)
-        got = _noalloc_cell_lists(gpu_lib, pos, H, comp_box, cutoff, ysort)
+        got = _noalloc_cell_lists(gpu_lib, pos, H, comp_box, cutoff, ysort, check_free=k > 0)
         assert got[2] == want[2]
         np.testing.assert_array_equal(got[1], want[1])
         np.testing.assert_array_equal(got[0], want[0])
+
+
+def test_noalloc_non_cubic_box_outside_particles_and_empty_input(gpu_lib):
+    """A non-cubic box (Mx, My, Mz differ, so the x + y Mx + z Mx My cell index matters), some
+    particles outside the chaining mesh (beyond the box, not listed: the counts sum to the
+    particles inside), and an empty input (every count 0), each against the allocating entry
+    point where it has one."""
+    H = 30.0 / 16
+    comp_box = (30.0, 22.5, 15.0)
+    cutoff = 3 * H
+    rng = np.random.default_rng(12)
+    pos = rng.uniform(0, 15.9, (4000, 3)).astype(np.float32)
+    pos[:, 1] *= np.float32(0.75)
+    pos[:, 2] *= np.float32(0.5)
+    pos[::37, 0] = np.float32(16.5)   # beyond the box in x (code units, box 16)
+    pos[5::41, 2] = np.float32(8.5)   # beyond the box in z (box 8)
+    # the first call on a device loads the scratch: make it before the memory checks (this
+    # test may run alone in a fresh process)
+    _noalloc_cell_lists(gpu_lib, pos[:10], H, comp_box, cutoff, 1)
+    for ysort in (1, 0):
+        want = _allocating_cell_lists(pos, H, comp_box, cutoff, ysort)
+        got = _noalloc_cell_lists(gpu_lib, pos, H, comp_box, cutoff, ysort, check_free=True)
+        assert got[2] == want[2] and len(set(got[2])) == 3
+        np.testing.assert_array_equal(got[1], want[1])
+        np.testing.assert_array_equal(got[0], want[0])
+        inside = ((pos[:, 0] < 16) & (pos[:, 1] < 12) & (pos[:, 2] < 8)).sum()
+        assert got[1].sum() == inside < len(pos)
+    empty = _noalloc_cell_lists(gpu_lib, np.zeros((0, 3), np.float32), H, comp_box, cutoff, 1,
+                                check_free=True)
+    assert len(empty[0]) == 0 and (empty[1] == 0).all()
 
 
 def test_noalloc_rejects_oversized_input(gpu_lib):
