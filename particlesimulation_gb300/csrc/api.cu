@@ -661,6 +661,32 @@ int p3m_create_internal(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out,
     const float totalForce = -Gc / (r * r + eps * eps);
     q->table_h[i] = r == 0 ? 0.0f : (totalForce - R) / std::sqrt(r * r + eps * eps);
   }
+  // the smooth part R(r)/r of the table-free force (shortRangeForce, source/p3mMethod.cpp:
+  // 220-238: (-G/r^2 + R(r)) / r per unit r_ij) at r^2 = i delta, in double, for the slotted
+  // pass's exact mode (pair.cu), which adds the Newton part -G/r^3 itself; its limit at r = 0
+  {
+    const double ad = a, Gd = 1.0 / (4.0 * std::numbers::pi), d2 = (double)re * re / 499.0;
+    auto Rd = [&](double r) -> double {
+      if (cfg->cloud_shape == PMGB_S1) {
+        if (r >= ad) return Gd / (r * r);
+        const double q1 = r / ad;
+        return Gd / (ad * ad) * (8 * q1 - 9 * q1 * q1 + 2 * q1 * q1 * q1 * q1);
+      }
+      const double u = 2 * r / ad;
+      if (u <= 1)
+        return Gd / (35 * ad * ad) * (224 * u - 224 * std::pow(u, 3) + 70 * std::pow(u, 4) + 48 * std::pow(u, 5) - 21 * std::pow(u, 6));
+      if (u <= 2)
+        return Gd / (35 * ad * ad) *
+               (12 / (u * u) - 224 + 896 * u - 840 * u * u + 224 * std::pow(u, 3) + 70 * std::pow(u, 4) -
+                48 * std::pow(u, 5) + 7 * std::pow(u, 6));
+      return Gd / (r * r);
+    };
+    const double g0 = cfg->cloud_shape == PMGB_S1 ? 8 * Gd / (ad * ad * ad) : 448 * Gd / (35 * ad * ad * ad);
+    for (int i = 0; i < 500; ++i) {
+      const double r = std::sqrt(i * d2);
+      q->table_h[500 + i] = (float)(i == 0 ? g0 : Rd(r) / r);
+    }
+  }
   q->pp.re2 = re * re;
   q->pp.re = re;
   q->pp.inv_d2 = 1.0f / q->delta2;
@@ -680,12 +706,12 @@ int p3m_create_internal(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out,
       (rc = dalloc(&q->scan_tmp, (size_t)scan_scratch_words((int)ntot))) ||
       (rc = dalloc(&q->items, (size_t)q->nitems_max)) ||
       (rc = dalloc(&q->heavy, (size_t)slot_heavy_capacity(q->nitems_max))) ||
-      (rc = dalloc(&q->table, 500)) || (rc = dalloc(&q->npairs, 1)) ||
+      (rc = dalloc(&q->table, 1000)) || (rc = dalloc(&q->npairs, 1)) ||
       (rc = dalloc(&q->slots, 27 * (size_t)std::max(pm->n, 1)))) {
     pmgb_p3m_destroy(q);
     return rc;
   }
-  if (cudaMemcpyAsync(q->table, q->table_h, 500 * sizeof(float), cudaMemcpyHostToDevice, pm->st) != cudaSuccess ||
+  if (cudaMemcpyAsync(q->table, q->table_h, 1000 * sizeof(float), cudaMemcpyHostToDevice, pm->st) != cudaSuccess ||
       cudaMemsetAsync(q->npairs, 0, sizeof(unsigned long long), pm->st) != cudaSuccess ||
       cudaStreamSynchronize(pm->st) != cudaSuccess) {
     pmgb_p3m_destroy(q);
@@ -784,7 +810,7 @@ int pmgb_p3m_pair_count(pmgb_p3m* q, unsigned long long* ordered_pairs) {
 
 int pmgb_p3m_get_sr_table(pmgb_p3m* q, float* table500, float* delta_sq) {
   if (!q) return set_error("null handle"), PMGB_EINVAL;
-  if (table500) std::memcpy(table500, q->table_h, sizeof(q->table_h));
+  if (table500) std::memcpy(table500, q->table_h, 500 * sizeof(float));
   if (delta_sq) *delta_sq = q->delta2;
   return PMGB_OK;
 }

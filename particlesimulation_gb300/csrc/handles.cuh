@@ -117,7 +117,7 @@ struct pmgb_p3m {
   int nitems_max = 0;             // capacity of items
   pmgb::u32* heavy = nullptr;     // heavy units of the table pass (slot_heavy_capacity entries)
   float* table = nullptr;
-  float table_h[500];
+  float table_h[1000];  // [0, 500): initSRForceTable; [500, 1000): R(r)/r for the exact mode
   float delta2 = 0;
   pmgb::PairParams pp{};
   unsigned long long* npairs = nullptr;

@@ -267,15 +267,35 @@ struct SlotI {
 // Positions are in units of sqrt(512) delta (relative to the slice's first particle), so |r|^2
 // is xs = xi / 512, saturated to [0, 1]; the table holds f / (sqrt(512) delta) for the scaled
 // difference vector, with the slopes times 512.
-template <bool EQM>
-__device__ __forceinline__ void slot_pair(SlotI& I, const float4& q, u32 tab_base) {
+// EXACT (the reference's table-free short-range force, useSRForceTable = false, softening 0):
+// positions in units of the cutoff, so xs = |r|^2 / re^2 saturated to [0, 1]; the smooth part
+// R(r)/r of the force comes from a 499-segment table in xs, the Newton part -G/r^3 exactly from
+// rsqrt: f = A[t] + xs S[t] + cn rsqrt(xs)^3, cn = -G m / re^2.  Segment 499 (xs = 1: at or
+// beyond the cutoff) holds A = -cn r3(1) with r3(1) computed by the same instructions, so the
+// two parts cancel there; |r|^2 starts from 1e-20 (not 0) so that the self pair (dx = dy = dz
+// = 0) has a finite f.
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+template <bool EQM, bool EXACT>
+__device__ __forceinline__ void slot_pair(SlotI& I, const float4& q, u32 tab_base, float cn) {
   const float dx = I.p.x - q.x, dy = I.p.y - q.y, dz = I.p.z - q.z;
   float xs;
-  asm("fma.rn.sat.f32 %0, %1, %1, %2;" : "=f"(xs) : "f"(dz), "f"(fmaf(dy, dy, dx * dx)));
-  const u32 bits = __float_as_uint(__fmaf_rd(xs, 512.0f, kMagic));  // kMagic + floor(512 xs)
+  asm("fma.rn.sat.f32 %0, %1, %1, %2;" : "=f"(xs)
+      : "f"(dz), "f"(fmaf(dy, dy, EXACT ? fmaf(dx, dx, 1e-20f) : dx * dx)));
+  // kMagic + floor(512 xs) (table) or kMagic + floor(499 xs) (exact): one rounding of the exact
+  // product, so the floor is exact
+  const u32 bits = __float_as_uint(__fmaf_rd(xs, EXACT ? 499.0f : 512.0f, kMagic));
   float2 ab;
   asm("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(ab.x), "=f"(ab.y) : "r"(bits * (SLOT_REP * 8) + tab_base));
   float f = fmaf(xs, ab.y, ab.x);
+  if (EXACT) {
+    const float ri = rsqrt_approx(xs);
+    f = fmaf(cn, ri * ri * ri, f);
+  }
   if (!EQM) f *= q.w;
   I.px = fmaf(f, dx, I.px);
   I.py = fmaf(f, dy, I.py);
@@ -338,6 +358,7 @@ struct SlotCtx {
   ChainDimsP cd;
   float re2, sc, gap_margin;
   int ysort;
+  float cn;  // EXACT: Newton coefficient -G m / re^2 in the scaled coordinates
 };
 
 // One work unit: the slice items[it / 27] against neighbour cell it % 27, into slot k of the
@@ -345,7 +366,7 @@ struct SlotCtx {
 // c = w, w + SLOT_WARPS, ... (chunks of 32 counted across the neighbour's sub-columns), and the
 // warps' partial sums are added in warp order through shared memory (part: SLOT_WARPS x
 // SLOT_SLICE), so the result does not depend on timing.
-template <bool EQM, bool COOP>
+template <bool EQM, bool EXACT, bool COOP>
 __device__ __forceinline__ void slot_unit(const SlotCtx& c, u32 it, float4 (*jbuf)[32], float4* part,
                                           u32 tab_base, int lane, int warp) {
   const ChainDimsP& cd = c.cd;
@@ -427,7 +448,7 @@ __device__ __forceinline__ void slot_unit(const SlotCtx& c, u32 it, float4 (*jbu
         for (int s = 0; s < cnt; ++s) {
           const float4 q = jbuf[warp][s];
 #pragma unroll
-          for (int u = 0; u < SLOT_IPL; ++u) slot_pair<EQM>(I[u], q, tab_base);
+          for (int u = 0; u < SLOT_IPL; ++u) slot_pair<EQM, EXACT>(I[u], q, tab_base, c.cn);
         }
         __syncwarp();
 #pragma unroll
@@ -472,7 +493,7 @@ __device__ __forceinline__ void slot_unit(const SlotCtx& c, u32 it, float4 (*jbu
 // others idle; then every warp takes the medium units (cost in [thr / 4, thr), listed from the
 // far end of the same buffer, counter[1]), then the rest in unit order (counter[8]).  If the
 // lists overflowed the buffer, every unit is taken by the last loop.
-template <bool EQM>
+template <bool EQM, bool EXACT>
 __global__ void __maxnreg__(128) pair_slot_kernel(
     const float4* __restrict__ pm, int n, const int* __restrict__ cell_start,
     const int2* __restrict__ items, const u32* __restrict__ nitems_p, const u32* __restrict__ heavy,
@@ -484,18 +505,40 @@ __global__ void __maxnreg__(128) pair_slot_kernel(
   float4 (*jbuf)[32] = reinterpret_cast<float4 (*)[32]>(slot_smem);
   float4* part = slot_smem + SLOT_WARPS * 32;
   float2* tab_all = reinterpret_cast<float2*>(part + SLOT_WARPS * SLOT_SLICE);
-  // coordinates are scaled by sc = 1/(sqrt(512) delta) (512 sc^2 = 1/delta^2 to float rounding)
-  const float sc = (float)sqrt((double)pp.inv_d2 / 512.0);
-  {
+  // table: coordinates are scaled by sc = 1/(sqrt(512) delta) (512 sc^2 = 1/delta^2 to float
+  // rounding); exact: by sc = 1/re
+  const float sc = EXACT ? 1.0f / pp.re : (float)sqrt((double)pp.inv_d2 / 512.0);
+  const double mj = EQM ? (double)__ldg(&pm[0].w) : 1.0;
+  float cn = 0.f;
+  if (!EXACT) {
     // every particle has the same mass when EQM: fold it into the table, with 1/sc
-    const double mj = (EQM ? (double)__ldg(&pm[0].w) : 1.0) / (double)sc;
+    const double mjs = mj / (double)sc;
     for (int t = threadIdx.x; t < SLOT_TAB; t += SLOT_THREADS) {
       float2 ab = make_float2(0.f, 0.f);
       if (t < 499) {
         const float a = table[t];
         const float s = table[t + 1] - a;
         const double A = (double)a - (double)t * (double)s;
-        ab = make_float2((float)(A * mj), (float)((double)s * 512.0 * mj));
+        ab = make_float2((float)(A * mjs), (float)((double)s * 512.0 * mjs));
+      }
+#pragma unroll
+      for (int c = 0; c < SLOT_REP; ++c) tab_all[t * SLOT_REP + c] = ab;
+    }
+  } else {
+    // smooth part g = R(r)/r at r^2 = t delta (table[500 + t], double-computed on the host),
+    // times m re, linear in xs = t / 499 per segment; segment 499 cancels the Newton part
+    const double G = 1.0 / (4.0 * 3.14159265358979323846), re = pp.re;
+    cn = (float)(-G * mj / (re * re));
+    const float r1 = rsqrt_approx(1.0f);
+    const float c499 = -(cn * (r1 * r1 * r1));
+    const double w = mj * re;
+    for (int t = threadIdx.x; t < SLOT_TAB; t += SLOT_THREADS) {
+      float2 ab = make_float2(0.f, 0.f);
+      if (t < 499) {
+        const double g0 = table[500 + t], g1 = table[500 + t + 1];
+        ab = make_float2((float)((g0 - (double)t * (g1 - g0)) * w), (float)((g1 - g0) * 499.0 * w));
+      } else if (t == 499) {
+        ab = make_float2(c499, 0.f);
       }
 #pragma unroll
       for (int c = 0; c < SLOT_REP; ++c) tab_all[t * SLOT_REP + c] = ab;
@@ -508,7 +551,7 @@ __global__ void __maxnreg__(128) pair_slot_kernel(
                        __float_as_uint(kMagic) * (u32)(SLOT_REP * 8);
   // a neighbour sub-column is skipped when its x-z distance from the slice's sub-column is at
   // least the cutoff (with a margin far above the rounding of the sub-column assignment)
-  const SlotCtx c{pm, cell_start, items, slots, n, cd, pp.re2, sc, 1e-3f * fminf(cd.HCsx, cd.HCsz), pp.ysort};
+  const SlotCtx c{pm, cell_start, items, slots, n, cd, pp.re2, sc, 1e-3f * fminf(cd.HCsx, cd.HCsz), pp.ysort, cn};
   const u32 nall = *nitems_p * NNB;  // every slice once per neighbour cell
   const u32 nh = __ldcg(&counter[2]), nm = __ldcg(&counter[3]);
   const bool listed = (unsigned long long)nh + nm <= heavy_cap;  // both lists complete
@@ -520,14 +563,14 @@ __global__ void __maxnreg__(128) pair_slot_kernel(
     const u32 h = s_unit;
     __syncthreads();
     if (h >= nheavy) break;
-    slot_unit<EQM, true>(c, __ldg(&heavy[h]), jbuf, part, tab_base, lane, warp);
+    slot_unit<EQM, EXACT, true>(c, __ldg(&heavy[h]), jbuf, part, tab_base, lane, warp);
   }
   for (;;) {
     u32 m = 0;
     if (lane == 0) m = atomicAdd(&counter[1], 1u);
     m = __shfl_sync(0xFFFFFFFFu, m, 0);
     if (m >= nmedium) break;
-    slot_unit<EQM, false>(c, __ldg(&heavy[heavy_cap - 1 - m]), jbuf, part, tab_base, lane, warp);
+    slot_unit<EQM, EXACT, false>(c, __ldg(&heavy[heavy_cap - 1 - m]), jbuf, part, tab_base, lane, warp);
   }
   for (;;) {
     u32 it = 0;
@@ -535,7 +578,7 @@ __global__ void __maxnreg__(128) pair_slot_kernel(
     it = __shfl_sync(0xFFFFFFFFu, it, 0);
     if (it >= nall) break;
     if (listed && slot_cost(cell_start, cd, items[it / NNB], (int)(it % NNB)) >= thr / 4) continue;
-    slot_unit<EQM, false>(c, it, jbuf, part, tab_base, lane, warp);
+    slot_unit<EQM, EXACT, false>(c, it, jbuf, part, tab_base, lane, warp);
   }
 }
 
@@ -656,7 +699,9 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
                 cudaStream_t st, int equal_mass, float4* slots, int n) {
   const int ncells = chd.Mx * chd.My * chd.Mz;
   const int ntot = ncells * chd.sub * chd.sub + 1;  // sub-columns + the bucket outside the mesh
-  const bool slotted = pp.use_table && !npairs && slots;
+  // the slotted pass: the table, or the exact table-free force without softening
+  const bool exact = !pp.use_table && pp.eps2 == 0.f;
+  const bool slotted = (pp.use_table || exact) && !npairs && slots;
   const int slice = slotted ? SLOT_SLICE : 32;
   item_count_kernel<<<(ntot + 255) / 256, 256, 0, st>>>(cell_start, ntot, item_cnt, slice, stop);
   int rc = exclusive_scan(item_cnt, item_off, ntot, nitems, scan_tmp, st);
@@ -675,20 +720,20 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
   if (ev_pair) PMGB_CUDA_TRY(cudaEventRecord(ev_pair, st));
   const dim3 grid(num_sms * 8), block(PAIR_THREADS);
   if (slotted) {  // table, staging and partial sums: 88.1 KB of dynamic shared memory
-    PMGB_CUDA_TRY(cudaFuncSetAttribute(pair_slot_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SLOT_SMEM));
-    PMGB_CUDA_TRY(cudaFuncSetAttribute(pair_slot_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SLOT_SMEM));
+    PMGB_CUDA_TRY(cudaFuncSetAttribute(pair_slot_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SLOT_SMEM));
+    PMGB_CUDA_TRY(cudaFuncSetAttribute(pair_slot_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SLOT_SMEM));
+    PMGB_CUDA_TRY(cudaFuncSetAttribute(pair_slot_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SLOT_SMEM));
+    PMGB_CUDA_TRY(cudaFuncSetAttribute(pair_slot_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SLOT_SMEM));
   }
 #define PMGB_PAIR_ARGS pm, vi, acc_pm, cell_start, items, nitems, counter, cd, pp, table, sp, kick, \
                        drift, kdk, pm_out, vi_out, acc_out, npairs, stop
   int launches = 3;  // item count, item build, pair pass (the scan counts itself)
   if (slotted) {
     if (nitems_max > 0) launches += 2;  // the two planning kernels
-    if (equal_mass)
-      pair_slot_kernel<true><<<num_sms * SLOT_CTAS_PER_SM, SLOT_THREADS, SLOT_SMEM, st>>>(
-          pm, n, cell_start, items, nitems, heavy, heavy_cap, counter, cd, pp, table, slots, stop);
-    else
-      pair_slot_kernel<false><<<num_sms * SLOT_CTAS_PER_SM, SLOT_THREADS, SLOT_SMEM, st>>>(
-          pm, n, cell_start, items, nitems, heavy, heavy_cap, counter, cd, pp, table, slots, stop);
+    auto kern = equal_mass ? (exact ? pair_slot_kernel<true, true> : pair_slot_kernel<true, false>)
+                           : (exact ? pair_slot_kernel<false, true> : pair_slot_kernel<false, false>);
+    kern<<<num_sms * SLOT_CTAS_PER_SM, SLOT_THREADS, SLOT_SMEM, st>>>(
+        pm, n, cell_start, items, nitems, heavy, heavy_cap, counter, cd, pp, table, slots, stop);
     if (n > 0)
       pair_epilogue_kernel<<<(n + 255) / 256, 256, 0, st>>>(pm, vi, acc_pm, slots, n, sp, kick, drift,
                                                             kdk, pm_out, vi_out, acc_out, stop);

@@ -3,7 +3,7 @@ compiled from the reference sources by oracle/Makefile).
 
 Run where the reference sources exist, naming the checkout:
     PSIM_REFERENCE=<reference checkout> python tests/golden/make_golden.py \
-        [diagnostics|recorder|samplers|field_sweeps|pm_accuracy]
+        [diagnostics|recorder|samplers|field_sweeps|pm_accuracy|p3m_exact]
 (with an argument, only that fixture is rewritten).
 Every case is a small seeded input; each fixture stores the inputs, the settings and the
 reference's outputs (float32), so tests on a machine without the reference still compare
@@ -258,6 +258,28 @@ def main():
     print("golden fixtures written to", HERE)
 
 
+def p3m_exact_fixture():
+    """The reference's table-free short-range force (useSRForceTable = false, softening 0:
+    shortRangeForce, source/p3mMethod.cpp:220-238) on the P3M inputs of p3m_forces.npz: S1 and
+    S2 shapes, y-sorted and unsorted chaining mesh, and a diameter below the cutoff (a = 2H,
+    re = 3H, so pairs at a <= r < re feel the pure Newtonian remainder)."""
+    H = 30.0 / 16
+    p, v, m = inputs(20, 3000, 4.0, 26.0)
+    cases = {"inputs": dict(pos=p, vel=v, mass=m)}
+    for cs, gf in ((0, 1), (1, 2)):
+        for ys in (1, 0):
+            for amul in (3.0, 2.0):
+                cfg = O.PMConfig(grid=(32, 32, 32), box=(30.0, 30.0, 30.0), H=H, DT=0.1, G=1.0,
+                                 interpolation=2, finite_diff=0, greens=gf, diameter=amul * H)
+                q = O.P3MConfig(comp_box=(30.0, 30.0, 30.0), cutoff=3 * H, diameter=amul * H,
+                                softening=0.0, cloud_shape=cs, use_table=0, y_sorting=ys)
+                acc = O.ref_p3m_accel(cfg, q, p, v, m)
+                cases[f"exact_cs{cs}_y{ys}_a{int(amul)}"] = dict(acc=acc, **_cfg_arrays(cfg),
+                                                                 **_p3m_arrays(q))
+    np.savez_compressed(os.path.join(HERE, "p3m_exact.npz"),
+                        **{f"{c}/{k}": a for c, dd in cases.items() for k, a in dd.items()})
+
+
 def pm_accuracy_fixture():
     """The reference's PM forces on the meshes of its accuracy scenario pmAccuracy
     (source/demos.cpp:361-428): a linear disk from DiskSamplerLinear(42) (centre (30, 30, 15),
@@ -307,6 +329,8 @@ if __name__ == "__main__":
         field_sweeps_fixture()
     elif sys.argv[1:] == ["pm_accuracy"]:
         pm_accuracy_fixture()
+    elif sys.argv[1:] == ["p3m_exact"]:
+        p3m_exact_fixture()
     else:
         main()
         diagnostics_fixture()
@@ -314,3 +338,4 @@ if __name__ == "__main__":
         samplers_fixture()
         field_sweeps_fixture()
         pm_accuracy_fixture()
+        p3m_exact_fixture()

@@ -43,6 +43,29 @@ def test_p3m_force_matches_reference_and_fp64(gpu_lib, case):
     pm.close()
 
 
+EXACT = load_npz("p3m_exact.npz")
+
+
+@pytest.mark.parametrize("case", [c for c in EXACT if c != "inputs"])
+def test_p3m_table_free_force(gpu_lib, case):
+    """useSRForceTable = false without softening: the slotted pass's exact mode (Newton part
+    from rsqrt, R(r)/r from a 499-segment table) against the FP64 oracle (1e-5) and the
+    reference's FP32 result (6e-5: the reference's own FP32 error here is ~4e-5)."""
+    d = EXACT[case]
+    inp = EXACT["inputs"]
+    cfg, q = cfg_from(d), p3m_from(d)
+    pm, p3m = make_p3m(cfg, q, inp["pos"], inp["vel"], inp["mass"])
+    p3m.force()
+    acc = pm.getParticles()[2].copy()
+    f64 = O.port_p3m_accel(cfg, q, inp["pos"], inp["vel"], inp["mass"], prec=1)
+    assert rel_rms(acc, f64) < 1e-5, "vs FP64 oracle"
+    assert rel_rms(acc, d["acc"]) < 6e-5, "vs reference FP32"
+    p3m.force()
+    np.testing.assert_array_equal(acc, pm.getParticles()[2])  # deterministic
+    p3m.close()
+    pm.close()
+
+
 @pytest.mark.parametrize("ys", [1, 0])
 def test_cell_lists_bit_exact(gpu_lib, ys):
     d = load_npz("cell_lists.npz")
