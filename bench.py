@@ -64,10 +64,12 @@ def parse():
                     help="skip the reference's own timing scenarios (run by the scenario CLI)")
     ap.add_argument("--no-pm-hbm", action="store_true",
                     help="skip the HBM-roofline measurement of the PM path on the 256^3 workload")
-    ap.add_argument("--closure-epochs", type=int, default=10)
+    ap.add_argument("--closure-epochs", type=int, default=60)
     ap.add_argument("--closure-bound", type=float, default=1e-3,
                     help="judge bound: median relative deviation from plain P3M (the target force "
                          "error)")
+    ap.add_argument("--no-reference-table", action="store_true",
+                    help="skip the closure comparison with the reference's 500-entry table")
     ap.add_argument("--no-disk-p3m", action="store_true",
                     help="skip the plain P3M measurement on the 262,144-particle disk")
     ap.add_argument("--seed", type=int, default=0)
@@ -436,18 +438,18 @@ def plain_headline(args, w, flush_l2, clocks, rank, world, brief=False):
 def closure_config(w, bound=1e-3):
     """config of the metric's workload, the same in both arms."""
     return {**config_of(w), "method": "P3M; learned short-range closure judged by plain P3M",
+            "short_range_force": "500-entry table" if w.p3m["table"] else
+            "exact formula (useSRForceTable = false)",
             "closure_pair_cutoff_cells": 0.5 * w.p3m["cutoff"] / w.H, "closure_bound": bound,
             "l2": "256 MB L2 flush before every timed step"}
 
 
-def closure_headline(args, w, flush_l2, clocks, rank, world):
-    """The metric's configuration: plain P3M vs the learned closure on the 1,048,576-particle
-    disk.  Set-up (untimed): training rows from the plain P3M at t = 0 and after 50 steps (2 x
-    1,048,576 rows), GPU training.  Then the force errors of plain P3M, the learned closure and
-    the reduced cutoff alone against an FP64 direct sum on 8,192 particles at the same positions,
-    each mode's own step time, and the headline: K steps of the judged run (the closure checked
-    by plain P3M every JUDGE_INTERVAL steps, fallback above args.closure_bound), CUDA events on
-    the handle's stream around each step, judge and fallback included."""
+def closure_setup(args, w, flush_l2):
+    """PM + learned closure on the workload, trained (untimed): training rows from the plain P3M
+    at t = 0 and after 50 steps (2 x N rows), GPU training.  Then, at the same positions, the
+    force errors of plain P3M, the learned closure and the reduced cutoff alone against an FP64
+    direct sum on ERR_TARGETS particles, the judge's median relative difference (learned vs
+    plain), and each mode's own step time (CUDA events on the handle's stream, L2 flushed)."""
     import numpy as np
 
     import particlesimulation_gb300 as P
@@ -458,7 +460,7 @@ def closure_headline(args, w, flush_l2, clocks, rank, world):
     q = w.p3m
     cl = P.LearnedClosure(pm, q["comp_box"], q["cutoff"], q["diameter"], q["softening"],
                           P.CloudShape(q["cloud_shape"]), 0.5 * q["cutoff"], capacity=2 * w.n,
-                          seed=args.seed)
+                          seed=args.seed, useSRForceTable=bool(q["table"]))
     t0 = time.perf_counter()
     cl.collect()
     pm.run(0)
@@ -467,7 +469,6 @@ def closure_headline(args, w, flush_l2, clocks, rank, world):
     t1 = time.perf_counter()
     loss = cl.train(epochs=args.closure_epochs, batch=2048, lr=2e-3)
     t2 = time.perf_counter()
-    # ---- force errors at the same positions: plain P3M, learned closure, reduced cutoff alone
     acc = {}
     for name, mode in (("plain_p3m", cl.FULL), ("learned_closure", cl.LEARNED),
                        ("reduced_cutoff_alone", cl.REDUCED_ONLY)):
@@ -481,6 +482,8 @@ def closure_headline(args, w, flush_l2, clocks, rank, world):
     a_pp = M.direct_sum_fp64(x, w.mass, w.G, idx)
     t4 = time.perf_counter()
     errors = {k: med_err(a[idx], a_pp) for k, a in acc.items()}
+    vs_plain = {k: med_err(acc[k][idx], acc["plain_p3m"][idx].astype(np.float64))
+                for k in ("learned_closure", "reduced_cutoff_alone")}
     cl.setMode(cl.LEARNED)
     judge = cl.judge(stride=JUDGE_STRIDE)
     stream = pm.stream()
@@ -501,8 +504,38 @@ def closure_headline(args, w, flush_l2, clocks, rank, world):
 
     ms_plain = mode_ms(cl.FULL, min(args.steps, 10))
     ms_learned = mode_ms(cl.LEARNED, min(args.steps, 10))
+    summary = {
+        "short_range_force": "500-entry table" if q["table"] else "exact formula (useSRForceTable = false)",
+        "judge_median_rel_diff_learned_vs_plain": judge,
+        "plain_p3m": {"value": w.n / (ms_plain * 1e-3), "ms_per_step": ms_plain,
+                      "force_err_vs_fp64_direct": errors["plain_p3m"]},
+        "learned_closure": {"value": w.n / (ms_learned * 1e-3), "ms_per_step": ms_learned,
+                            "force_err_vs_fp64_direct": errors["learned_closure"],
+                            "force_diff_vs_plain_p3m": vs_plain["learned_closure"]},
+        "reduced_cutoff_alone": {"force_err_vs_fp64_direct": errors["reduced_cutoff_alone"],
+                                 "force_diff_vs_plain_p3m": vs_plain["reduced_cutoff_alone"]},
+        "learned_speedup_unjudged": ms_plain / ms_learned,
+        "training": {"rows": rows, "epochs": args.closure_epochs, "final_mse": loss,
+                     "collect_s": round(t1 - t0, 2), "train_s": round(t2 - t1, 2)},
+        "direct_sum": {"targets": ERR_TARGETS, "sources": w.n, "seconds": round(t4 - t3, 3),
+                       "precision": "fp64", "device": "gpu (pmgb_direct_sum_fp64)"}}
+    return pm, cl, summary
 
-    # ---- the headline: the judged run
+
+def closure_headline(args, w, flush_l2, clocks, rank, world):
+    """The metric's configuration: plain P3M vs the learned closure on the 1,048,576-particle
+    disk (closure_setup), then the headline: K steps of the judged run (the closure checked by
+    plain P3M every JUDGE_INTERVAL steps, fallback to plain P3M above args.closure_bound), CUDA
+    events on the handle's stream around each step, judge and fallback included; e2e through the
+    C ABI; the roofline of the full-cutoff pair pass; the same comparison with the reference's
+    500-entry table (closure.reference_table)."""
+    import particlesimulation_gb300 as P
+    from particlesimulation_gb300 import methods as M
+    from particlesimulation_gb300 import workloads as W
+    pm, cl, summary = closure_setup(args, w, flush_l2)
+    stream = pm.stream()
+    q = w.p3m
+
     def judged_step(s):
         iv = 1 if s % JUDGE_INTERVAL == 0 else 0  # judge before this step (learned mode only)
         esc, _, fb, _ = cl.run(1, args.closure_bound, iv, JUDGE_STRIDE)
@@ -537,36 +570,32 @@ def closure_headline(args, w, flush_l2, clocks, rank, world):
     cl.setMode(cl.LEARNED)
     e2e = e2e_steps(pm, args.steps, judged_step, world, w.n)
     cl.close()
-    # ---- roofline of the dominant kernel: the full-cutoff pair pass (what the judged run runs
-    # after a fallback), on a plain P3M handle over the same positions
+    # roofline of the dominant kernel of plain P3M: the full-cutoff pair pass, on a plain P3M
+    # handle over the same positions
     p3m = P.P3MMethod(pm, q["comp_box"], q["cutoff"], q["diameter"], w.H, q["softening"],
                       P.CloudShape(q["cloud_shape"]), bool(q["table"]), bool(q["ysort"]))
     roofline, stage = pair_roofline(pm, p3m, flush_l2, M.fp32_peak_tflops())
     p3m.close()
     pm.close()
+    ms_plain = summary["plain_p3m"]["ms_per_step"]
+    closure = {"bound": args.closure_bound, "judge_interval": JUDGE_INTERVAL,
+               "judge_stride": JUDGE_STRIDE, "fallback_step": fallback,
+               "mode_after_run": final_mode, **summary,
+               "judged_speedup_vs_plain": ms_plain / ms_step,
+               "target_met": bool(summary["learned_closure"]["force_err_vs_fp64_direct"]["median"]
+                                  <= args.closure_bound and ms_plain / ms_step >= 2.0)}
+    if not args.no_reference_table:  # the same comparison with the reference's table
+        wt = W.disk_p3m_1m(table=1)
+        pmt, clt, st = closure_setup(args, wt, flush_l2)
+        clt.close()
+        pmt.close()
+        closure["reference_table"] = st
     cpu = cpu_baseline_obj(w, args, rank, world)
-    bound = args.closure_bound
-    closure = {
-        "bound": bound, "judge": {"interval": JUDGE_INTERVAL, "stride": JUDGE_STRIDE,
-                                  "median_rel_diff_learned_vs_plain": judge},
-        "fallback_step": fallback, "mode_after_run": final_mode,
-        "plain_p3m": {"value": w.n / (ms_plain * 1e-3), "ms_per_step": ms_plain,
-                      "force_err_vs_fp64_direct": errors["plain_p3m"]},
-        "learned_closure": {"value": w.n / (ms_learned * 1e-3), "ms_per_step": ms_learned,
-                            "force_err_vs_fp64_direct": errors["learned_closure"]},
-        "reduced_cutoff_alone": {"force_err_vs_fp64_direct": errors["reduced_cutoff_alone"]},
-        "learned_speedup_unjudged": ms_plain / ms_learned,
-        "judged_speedup_vs_plain": ms_plain / ms_step,
-        "target_met": bool(errors["learned_closure"]["median"] <= bound and ms_plain / ms_step >= 2.0),
-        "training": {"rows": rows, "epochs": args.closure_epochs, "final_mse": loss,
-                     "collect_s": round(t1 - t0, 2), "train_s": round(t2 - t1, 2)},
-        "direct_sum": {"targets": ERR_TARGETS, "sources": w.n, "seconds": round(t4 - t3, 3),
-                       "precision": "fp64", "device": "gpu (pmgb_direct_sum_fp64)"}}
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generator, particlesimulation_gb300/workloads.py)",
-            "config": closure_config(w, bound), "e2e": e2e, "roofline": roofline,
+            "config": closure_config(w, args.closure_bound), "e2e": e2e, "roofline": roofline,
             "stage_ms_plain": {k: round(v, 4) for k, v in stage.items()}, "cpu_baseline": cpu,
             "clocks": clk, "gpu_launches": launches, "closure": closure, "impl": "ours"}
 

@@ -9,7 +9,8 @@ arrays.  State layout follows the reference's constructors: N positions then N v
                     TSC, S2 shapes, cutoff 3 mesh cells                           (C1)
   blobs_periodic    PM, 4,194,304 particles uniform + 64 Gaussian blobs, periodic
                     256^3, CIC                                                    (C2)
-  disk_p3m_1m       C1's generator at 1,048,576 particles (learned closure)       (C4)
+  disk_p3m_1m       C1's generator at 1,048,576 particles, exact short-range formula
+                    (learned closure)                                             (C4)
 """
 from __future__ import annotations
 
@@ -133,10 +134,11 @@ def plummer_cluster(n=16384, seed=0, grid=64):
                     (grid,) * 3, (box,) * 3, box / (grid // 2), 0.01, 1.0, 1, 0, 0, 0.0, 100)
 
 
-def disk_p3m(n=262144, seed=1, grid=128, cutoff_cells=3.0):
+def disk_p3m(n=262144, seed=1, grid=128, cutoff_cells=3.0, table=1):
     """C1: disk + bulge in a side-60 box, mesh 128^3 of twice the box (H = 60/64), TSC,
     S2-optimal influence function with particle diameter = cutoff = 3 H, plain P3M with the
-    500-entry table and y-sorted chaining mesh; dt = 0.005, 200 steps."""
+    500-entry table (table = 0: the exact short-range formula, useSRForceTable = false) and
+    y-sorted chaining mesh; dt = 0.005, 200 steps."""
     rng = np.random.default_rng(seed)
     p, v = disk_bulge(rng, n)
     box = 60.0
@@ -145,7 +147,7 @@ def disk_p3m(n=262144, seed=1, grid=128, cutoff_cells=3.0):
     return Workload("disk_p3m", _f32(p + box / 2), _f32(v), _f32(np.full(n, 1.0 / n)),
                     (grid,) * 3, (box,) * 3, H, 0.005, 1.0, 2, 0, 2, a, 200,
                     p3m=dict(comp_box=(box,) * 3, cutoff=cutoff_cells * H, diameter=a,
-                             softening=0.0, cloud_shape=1, table=1, ysort=1))
+                             softening=0.0, cloud_shape=1, table=table, ysort=1))
 
 
 def blobs_periodic(n=4194304, seed=2, grid=256):
@@ -158,9 +160,12 @@ def blobs_periodic(n=4194304, seed=2, grid=256):
                     periodic=True)
 
 
-def disk_p3m_1m(n=1048576, seed=4, grid=128, cutoff_cells=3.0):
-    """C4: C1's generator at 1,048,576 particles."""
-    w = disk_p3m(n=n, seed=seed, grid=grid, cutoff_cells=cutoff_cells)
+def disk_p3m_1m(n=1048576, seed=4, grid=128, cutoff_cells=3.0, table=0):
+    """C4: C1's generator at 1,048,576 particles, the learned closure's workload.  By default
+    with the exact short-range formula (the reference's useSRForceTable = false): the 500-entry
+    table's error on close pairs (F(0) = 0, linear in r^2) sits in every residual the closure
+    is trained on and is larger than the closure's own error; table = 1 keeps the table."""
+    w = disk_p3m(n=n, seed=seed, grid=grid, cutoff_cells=cutoff_cells, table=table)
     w.name = "disk_p3m_1m"
     return w
 

