@@ -106,7 +106,8 @@ def run_profile_closure(args):
     pm, _ = make_system(W.Workload(**{**w.__dict__, "p3m": None}))
     q = w.p3m
     cl = P.LearnedClosure(pm, q["comp_box"], q["cutoff"], q["diameter"], q["softening"],
-                          P.CloudShape(q["cloud_shape"]), 0.5 * q["cutoff"], seed=args.seed)
+                          P.CloudShape(q["cloud_shape"]), 0.5 * q["cutoff"], seed=args.seed,
+                          useSRForceTable=bool(q["table"]))
     cl.setMode(cl.LEARNED)
     pm.run(0)
     _, _, ms = pm.advance(args.profile_closure)

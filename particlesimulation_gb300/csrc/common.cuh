@@ -141,6 +141,10 @@ __device__ __forceinline__ void fx_add_global(u64* p, long long v) {
   atomicAdd(p, (u64)v);
 }
 
+// powers of two only: one AND, exact for any a (the interpolation's potential reads, where the
+// general form below measured 30 % slower at 256^3)
+__device__ __forceinline__ int wrapi_p2(int a, int n) { return a & (n - 1); }
+
 __device__ __forceinline__ int wrapi(int a, int n) {
   // a mesh index wrapped into [0, n).  Powers of two: one AND, exact for any a.  Other sizes
   // (the mixed-radix meshes): a is at most a stencil width outside the mesh for particles inside

@@ -17,7 +17,7 @@
 
 namespace pmgb {
 
-template <int IS, int FDS, bool KDK>
+template <int IS, int FDS, bool KDK, bool POW2>
 __global__ void __launch_bounds__(256) interp_kernel(float4* __restrict__ pm, float4* __restrict__ vi,
                                                      float4* __restrict__ acc, int n,
                                                      const float* __restrict__ phi, StepParams sp,
@@ -25,17 +25,18 @@ __global__ void __launch_bounds__(256) interp_kernel(float4* __restrict__ pm, fl
   if (stopped_before(stop, KDK && drift, sp.step_tag)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  interp_particle<IS, FDS, KDK>(pm, vi, acc, i, phi, sp, kick, drift, stop);
+  interp_particle<IS, FDS, KDK, POW2>(pm, vi, acc, i, phi, sp, kick, drift, stop);
 }
 
 template <int IS, int FDS>
 static void launch_interp_t(bool kdk, float4* pm, float4* vi, float4* acc, int n, const float* phi,
                             const StepParams& sp, float kick, int drift, int* stop, cudaStream_t st) {
   const int blocks = (n + 255) / 256;
-  if (kdk)
-    interp_kernel<IS, FDS, true><<<blocks, 256, 0, st>>>(pm, vi, acc, n, phi, sp, kick, drift, stop);
-  else
-    interp_kernel<IS, FDS, false><<<blocks, 256, 0, st>>>(pm, vi, acc, n, phi, sp, kick, drift, stop);
+  const MeshDims& m = sp.m;
+  const bool p2 = !(m.nx & (m.nx - 1)) && !(m.ny & (m.ny - 1)) && !(m.nz & (m.nz - 1));
+  auto k = kdk ? (p2 ? interp_kernel<IS, FDS, true, true> : interp_kernel<IS, FDS, true, false>)
+               : (p2 ? interp_kernel<IS, FDS, false, true> : interp_kernel<IS, FDS, false, false>);
+  k<<<blocks, 256, 0, st>>>(pm, vi, acc, n, phi, sp, kick, drift, stop);
 }
 
 int launch_interp(bool kdk, float4* pm, float4* vi, float4* acc, int n, const float* phi,

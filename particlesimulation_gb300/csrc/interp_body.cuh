@@ -5,17 +5,21 @@
 
 namespace pmgb {
 
+template <bool POW2>
 __device__ __forceinline__ float phi_at(const float* __restrict__ phi, const MeshDims& m, int x,
                                         int y, int z) {
+  if (POW2)
+    return __ldg(&phi[((size_t)wrapi_p2(z, m.nz) * m.ny + wrapi_p2(y, m.ny)) * m.nx + wrapi_p2(x, m.nx)]);
   return __ldg(&phi[((size_t)wrapi(z, m.nz) * m.ny + wrapi(y, m.ny)) * m.nx + wrapi(x, m.nx)]);
 }
 
 // Where the potential is read: the mesh in global memory, indices wrapped periodically as in
-// Grid::getPotential (reference source/grid.cpp:66-68).
+// Grid::getPotential (reference source/grid.cpp:66-68); POW2: every side a power of two.
+template <bool POW2>
 struct PhiGlobal {
   const float* __restrict__ phi;
   MeshDims m;
-  __device__ __forceinline__ float operator()(int x, int y, int z) const { return phi_at(phi, m, x, y, z); }
+  __device__ __forceinline__ float operator()(int x, int y, int z) const { return phi_at<POW2>(phi, m, x, y, z); }
 };
 
 template <int FDS, class Phi>
@@ -111,12 +115,12 @@ __device__ __forceinline__ void interp_particle_p(float4* __restrict__ pm, float
   }
 }
 
-template <int IS, int FDS, bool KDK>
+template <int IS, int FDS, bool KDK, bool POW2 = true>
 __device__ __forceinline__ void interp_particle(float4* __restrict__ pm, float4* __restrict__ vi,
                                                 float4* __restrict__ acc, int i,
                                                 const float* __restrict__ phi, const StepParams& sp,
                                                 float kick, int drift, int* stop) {
-  interp_particle_p<IS, FDS, KDK>(pm, vi, acc, i, pm[i], PhiGlobal{phi, sp.m}, sp, kick, drift, stop);
+  interp_particle_p<IS, FDS, KDK>(pm, vi, acc, i, pm[i], PhiGlobal<POW2>{phi, sp.m}, sp, kick, drift, stop);
 }
 
 }  // namespace pmgb
