@@ -348,8 +348,12 @@ int pmgb_closure_train(pmgb_closure* c, int epochs, int batch, float lr, float* 
 int pmgb_closure_param_count(void);
 int pmgb_closure_get_params(pmgb_closure* c, float* params, int count);
 int pmgb_closure_set_params(pmgb_closure* c, const float* params, int count);
-/* Median relative difference between the learned and the full-cutoff P3M accelerations over
- * every `stride`-th particle at the current positions. */
+/* Median relative difference between the learned and the full-cutoff P3M accelerations at the
+ * current positions, over the particles of every `stride`-th slice (64 particles of a chaining-
+ * mesh sub-column) of the full-cutoff pair pass, which then covers only those slices (about
+ * 1/stride of its cost); with the table-free formula and softening, over every `stride`-th
+ * particle by index (full pass).  The learned force is the last step's when that step was
+ * learned and the particles have not moved since. */
 int pmgb_closure_judge(pmgb_closure* c, int stride, float* median_rel_err);
 /* n_steps run-loop iterations in the current mode; in PMGB_CLOSURE_LEARNED the judge runs every
  * judge_interval steps and a median error above `bound` switches the rest of the run to plain

@@ -95,6 +95,7 @@ int check_cfg(const pmgb_pm_config* c, int n) {
 
 int upload_state(pmgb_pm* h, const float* pos, const float* vel, int units) {
   const size_t n = (size_t)h->n;
+  h->acc_mode = -1;
   if (n == 0) return PMGB_OK;
   PMGB_CUDA_TRY(cudaMemcpyAsync(h->stage, pos, 3 * n * sizeof(float), cudaMemcpyHostToDevice, h->st));
   PMGB_CUDA_TRY(cudaMemcpyAsync(h->stage + 3 * n, vel, 3 * n * sizeof(float), cudaMemcpyHostToDevice, h->st));
@@ -185,6 +186,7 @@ int force(pmgb_pm* h, int kdk, float kick, int drift, int tag, bool timed) {
       cudaEventRecord(h->ev[4], h->st);
       cudaEventRecord(h->ev[5], h->st);
     }
+    h->acc_mode = (kdk && drift) ? -1 : closure_mode(h);
     return PMGB_OK;
   }
   rc = launch_interp(false, h->pm[h->cur], h->vi[h->cur], h->acc_pm, n, h->phi, sp, kick, drift, stop, h->st);
@@ -199,13 +201,17 @@ int force(pmgb_pm* h, int kdk, float kick, int drift, int tag, bool timed) {
                    q->counter, q->pp, q->table, sp,
                    kick, drift, kdk, h->pm[1 - h->cur], h->vi[1 - h->cur], h->acc,
                    q->count_pairs ? q->npairs : nullptr, stop,
-                   h->num_sms, timed ? h->ev[4] : nullptr, h->st, h->equal_mass, q->slots, n);
+                   h->num_sms, timed ? h->ev[4] : nullptr, h->st, h->equal_mass, q->slots, n,
+                   q->unit_stride);
   if (rc) return rc;
   if (kdk) {
     h->cur = 1 - h->cur;
     // acc was written in the order of the particles just moved into h->cur: same slots
   }
   if (timed) cudaEventRecord(h->ev[5], h->st);
+  // a drift after the force leaves accelerations that belong to the old positions; a sampled
+  // pair pass leaves most of them incomplete
+  h->acc_mode = (kdk && drift) || q->unit_stride > 1 ? -1 : closure_mode(h);
   return PMGB_OK;
 }
 
@@ -255,7 +261,9 @@ int run_loop(pmgb_pm* h, int sim_length, int* steps_done) {
   int flags[3];
   PMGB_CUDA_TRY(cudaMemcpyAsync(flags, h->flags, 3 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
   PMGB_CUDA_TRY(cudaStreamSynchronize(h->st));
-  return run_status(flags, steps_done, sim_length + 1);
+  rc = run_status(flags, steps_done, sim_length + 1);
+  if (rc) h->acc_mode = -1;  // stopped after a drift whose force was skipped
+  return rc;
 }
 
 }  // namespace
@@ -473,7 +481,9 @@ int pmgb_pm_advance(pmgb_pm* h, int n_steps, int* steps_done, float* device_ms) 
   PMGB_CUDA_TRY(cudaMemcpyAsync(flags, h->flags, 3 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
   PMGB_CUDA_TRY(cudaStreamSynchronize(h->st));
   if (device_ms) cudaEventElapsedTime(device_ms, h->ev[0], h->ev[5]);
-  return run_status(flags, steps_done, n_steps);
+  rc0 = run_status(flags, steps_done, n_steps);
+  if (rc0) h->acc_mode = -1;  // stopped after a drift whose force was skipped
+  return rc0;
 }
 
 int pmgb_pm_run_recorded(pmgb_pm* h, pmgb_recorder* rec, int sim_length, int collect_diagnostics,

@@ -885,6 +885,7 @@ struct pmgb_closure {
   int cap = 0, count = 0;
   float* accF = nullptr;        // scratch: 3n floats each
   float* accR = nullptr;
+  unsigned char* judged = nullptr;  // n flags: particles a sampled judge pass covered
   int adam_t = 0;
   unsigned long long seed = 0;
 };
@@ -918,6 +919,8 @@ int closure_apply(pmgb_pm* h) {
   }
   return PMGB_OK;
 }
+
+int closure_mode(const pmgb_pm* h) { return h->closure ? h->closure->mode : 3; }
 
 static void set_mode(pmgb_closure* c, int mode) {
   c->mode = mode;
@@ -996,7 +999,7 @@ int pmgb_closure_create(pmgb_pm* pm, const pmgb_p3m_config* full_cfg, float redu
       (rc = cl_alloc(&c->loss, 1)) || (rc = cl_alloc(&c->img, IMG_SIZE)) ||
       (rc = cl_alloc(&c->X, (size_t)std::max(c->cap, 1) * CL_K0)) ||
       (rc = cl_alloc(&c->T, (size_t)std::max(c->cap, 1) * 4)) || (rc = cl_alloc(&c->accF, 3 * n)) ||
-      (rc = cl_alloc(&c->accR, 3 * n))) {
+      (rc = cl_alloc(&c->accR, 3 * n)) || (rc = cl_alloc(&c->judged, n))) {
     pmgb_closure_destroy(c);
     return rc;
   }
@@ -1032,7 +1035,7 @@ int pmgb_closure_destroy(pmgb_closure* c) {
   if (c->full) pmgb_p3m_destroy(c->full);
   if (c->reduced) pmgb_p3m_destroy(c->reduced);
   void* ptrs[] = {c->occ_fx, c->occ, c->params, c->adam_m, c->adam_v, c->grad, c->gw, c->lossw,
-                  c->loss, c->img, c->X, c->T, c->accF, c->accR};
+                  c->loss, c->img, c->X, c->T, c->accF, c->accR, c->judged};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete c;
@@ -1151,17 +1154,44 @@ int pmgb_closure_judge(pmgb_closure* c, int stride, float* median_rel_err) {
   if (!c || !median_rel_err) return set_error("null argument"), PMGB_EINVAL;
   if (stride < 1) stride = 1;
   pmgb_pm* h = c->pm;
-  int rc = force_into(c, PMGB_CLOSURE_LEARNED, c->accR);
-  if (rc) return rc;
-  rc = force_into(c, PMGB_CLOSURE_FULL, c->accF);
-  if (rc) return rc;
   const size_t n = (size_t)h->n;
+  int rc;
+  // the learned force at the current positions: the one the last step left when it was a
+  // learned step, else a fresh evaluation
+  if (h->acc_mode == PMGB_CLOSURE_LEARNED) {
+    rc = launch_unpack(h->pm[h->cur], h->vi[h->cur], h->acc, h->n, h->cfg.H, h->cfg.DT, 0, h->stage,
+                       h->stage + 3 * n, h->stage + 6 * n, h->st);
+    if (rc) return rc;
+    PMGB_CUDA_TRY(cudaMemcpyAsync(c->accR, h->stage + 6 * n, 3 * n * sizeof(float), cudaMemcpyDeviceToDevice,
+                                  h->st));
+  } else if ((rc = force_into(c, PMGB_CLOSURE_LEARNED, c->accR))) {
+    return rc;
+  }
+  // the plain P3M force on the particles of every stride-th slice of its pair pass (a sampled
+  // pass, about 1/stride of its cost), or on every stride-th particle where the pass cannot be
+  // sampled (the direct formula with softening)
+  const bool sampled = stride > 1 && pair_pass_sampleable(c->full->pp);
+  c->full->unit_stride = sampled ? stride : 1;
+  rc = force_into(c, PMGB_CLOSURE_FULL, c->accF);
+  c->full->unit_stride = 1;
+  if (rc) return rc;
+  std::vector<unsigned char> flag(n, 0);
+  if (sampled && n) {
+    PMGB_CUDA_TRY(cudaMemsetAsync(c->judged, 0, n, h->st));
+    rc = launch_mark_sampled(c->full->cell_start, c->full->items, c->full->nitems, c->full->nitems_max, stride,
+                             h->vi[h->cur], c->judged, h->st);
+    if (rc) return rc;
+    PMGB_CUDA_TRY(cudaMemcpyAsync(flag.data(), c->judged, n, cudaMemcpyDeviceToHost, h->st));
+  } else {
+    for (size_t i = 0; i < n; i += (size_t)stride) flag[i] = 1;
+  }
   std::vector<float> a(3 * n), b(3 * n);
   PMGB_CUDA_TRY(cudaMemcpyAsync(a.data(), c->accR, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, h->st));
   PMGB_CUDA_TRY(cudaMemcpyAsync(b.data(), c->accF, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, h->st));
   PMGB_CUDA_TRY(cudaStreamSynchronize(h->st));
   std::vector<float> e;
-  for (size_t i = 0; i < n; i += (size_t)stride) {
+  for (size_t i = 0; i < n; ++i) {
+    if (!flag[i]) continue;
     const double dx = a[3 * i] - b[3 * i], dy = a[3 * i + 1] - b[3 * i + 1], dz = a[3 * i + 2] - b[3 * i + 2];
     const double nb = std::sqrt((double)b[3 * i] * b[3 * i] + (double)b[3 * i + 1] * b[3 * i + 1] +
                                 (double)b[3 * i + 2] * b[3 * i + 2]);

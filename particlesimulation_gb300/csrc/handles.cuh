@@ -52,7 +52,12 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
                 int nitems_max, u32* heavy, u32* counter, const PairParams& pp, const float* table,
                 const StepParams& sp, float kick, int drift, int kdk, float4* pm_out, float4* vi_out,
                 float4* acc_out, unsigned long long* npairs, int* stop, int num_sms, cudaEvent_t ev_pair,
-                cudaStream_t st, int equal_mass, float4* slots, int n);
+                cudaStream_t st, int equal_mass, float4* slots, int n, int unit_stride = 1);
+// Sampled pair passes (unit_stride > 1, slotted passes only: pair_pass_sampleable): flags[id] = 1
+// for the particles of the slices such a pass covered (original index order).
+bool pair_pass_sampleable(const PairParams& pp);
+int launch_mark_sampled(const int* cell_start, const int2* items, const u32* nitems, int nitems_max,
+                        int unit_stride, const float4* vi, unsigned char* flags, cudaStream_t st);
 
 }  // namespace pmgb
 
@@ -100,6 +105,8 @@ struct pmgb_pm {
   pmgb_recorder* rec = nullptr;  // recorder of the current pmgb_pm_run_recorded, else null
   int rec_field = 0;
   float4* ivel = nullptr;  // integer-step velocities, original order (pmgb_pm_leapfrog), lazily
+  // the closure mode whose force h->acc holds at the current positions (-1: none; 3: no closure)
+  int acc_mode = -1;
   bool generic = false;    // mesh not all powers of two in [8, 512]: mixed-radix Poisson solve
   void* gplans = nullptr;  // its plans (gfft.cu)
 };
@@ -123,12 +130,15 @@ struct pmgb_p3m {
   unsigned long long* npairs = nullptr;
   int count_pairs = 0;  // count in-range pairs during force evaluations (pmgb_p3m_set_pair_counting)
   float4* slots = nullptr;  // 27 x n partial short-range accelerations (pair.cu, table pass)
+  int unit_stride = 1;      // > 1: the next passes cover every unit_stride-th slice only (judge)
 };
 
 namespace pmgb {
 // Adds the closure's predicted residual short-range acceleration to h->acc_pm (sorted order of
 // h->pm[h->cur]); defined in closure.cu.
 int closure_apply(pmgb_pm* h);
+// The closure mode of h's force evaluations (PMGB_CLOSURE_*), 3 without a closure (closure.cu).
+int closure_mode(const pmgb_pm* h);
 // P3M handle over pm; attach = make it pm's pair pass (api.cu).
 int p3m_create_internal(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out, bool attach);
 

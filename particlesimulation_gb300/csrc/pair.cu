@@ -498,7 +498,7 @@ __global__ void __maxnreg__(128) pair_slot_kernel(
     const float4* __restrict__ pm, int n, const int* __restrict__ cell_start,
     const int2* __restrict__ items, const u32* __restrict__ nitems_p, const u32* __restrict__ heavy,
     u32 heavy_cap, u32* __restrict__ counter, ChainDimsP cd, PairParams pp, const float* __restrict__ table,
-    float4* __restrict__ slots, const int* __restrict__ stop) {
+    float4* __restrict__ slots, u32 unit_stride, const int* __restrict__ stop) {
   if (*stop) return;
   extern __shared__ float4 slot_smem[];
   __shared__ u32 s_unit;
@@ -577,6 +577,7 @@ __global__ void __maxnreg__(128) pair_slot_kernel(
     if (lane == 0) it = atomicAdd(&counter[8], 1u);
     it = __shfl_sync(0xFFFFFFFFu, it, 0);
     if (it >= nall) break;
+    if ((it / NNB) % unit_stride) continue;  // sampled pass: every unit_stride-th slice only
     if (listed && slot_cost(cell_start, cd, items[it / NNB], (int)(it % NNB)) >= thr / 4) continue;
     slot_unit<EQM, EXACT, false>(c, it, jbuf, part, tab_base, lane, warp);
   }
@@ -642,11 +643,11 @@ constexpr int SLOT_COUNTER_WORDS = 10;
 // Total estimated cost of all units (one thread per item, its 27 neighbour cells).
 __global__ void plan_cost_kernel(const int* __restrict__ cell_start, const int2* __restrict__ items,
                                  const u32* __restrict__ nitems_p, ChainDimsP cd, u32* __restrict__ counter,
-                                 const int* stop) {
+                                 u32 unit_stride, const int* stop) {
   if (*stop) return;
   const u32 item = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long s = 0;
-  if (item < *nitems_p) {
+  if (item < *nitems_p && item % unit_stride == 0) {
     const int2 it = items[item];
     for (int k = 0; k < NNB; ++k) s += slot_cost(cell_start, cd, it, k);
   }
@@ -661,14 +662,14 @@ __global__ void plan_cost_kernel(const int* __restrict__ cell_start, const int2*
 __global__ void plan_heavy_kernel(const int* __restrict__ cell_start, const int2* __restrict__ items,
                                   const u32* __restrict__ nitems_p, ChainDimsP cd,
                                   u32* __restrict__ heavy, u32 cap, u32* __restrict__ counter,
-                                  unsigned long long warps, const int* stop) {
+                                  unsigned long long warps, u32 unit_stride, const int* stop) {
   if (*stop) return;
   const unsigned long long total = __ldcg(reinterpret_cast<const unsigned long long*>(counter + 4));
   const unsigned long long t = total / (warps * SLOT_HEAVY_DIV);
   const unsigned long long thr = t > SLOT_HEAVY_MIN ? t : SLOT_HEAVY_MIN;
   const u32 item = blockIdx.x * blockDim.x + threadIdx.x;
   if (item == 0) *reinterpret_cast<unsigned long long*>(counter + 6) = thr;
-  if (item >= *nitems_p) return;
+  if (item >= *nitems_p || item % unit_stride) return;
   const int2 it = items[item];
   for (int k = 0; k < NNB; ++k) {
     const unsigned long long cost = slot_cost(cell_start, cd, it, k);
@@ -681,6 +682,30 @@ __global__ void plan_heavy_kernel(const int* __restrict__ cell_start, const int2
     }
   }
 }
+
+// The particles a sampled pass (unit_stride > 1) covers: those of every unit_stride-th slice,
+// flagged in original index order (flags cleared by the caller).
+__global__ void mark_sampled_kernel(const int* __restrict__ cell_start, const int2* __restrict__ items,
+                                    const u32* __restrict__ nitems_p, u32 unit_stride,
+                                    const float4* __restrict__ vi, unsigned char* __restrict__ flags) {
+  const u32 k = (blockIdx.x * blockDim.x + threadIdx.x) * unit_stride;
+  if (k >= *nitems_p) return;
+  const int2 it = items[k];
+  const int end = min(it.y + SLOT_SLICE, cell_start[it.x + 1]);
+  for (int i = it.y; i < end; ++i) flags[__float_as_int(vi[i].w)] = 1;
+}
+
+int launch_mark_sampled(const int* cell_start, const int2* items, const u32* nitems, int nitems_max,
+                        int unit_stride, const float4* vi, unsigned char* flags, cudaStream_t st) {
+  const int nk = (nitems_max + unit_stride - 1) / unit_stride;
+  if (nk > 0) mark_sampled_kernel<<<(nk + 255) / 256, 256, 0, st>>>(cell_start, items, nitems, (u32)unit_stride,
+                                                                    vi, flags);
+  PMGB_LAUNCH_CHECK();
+  count_launches(1);
+  return PMGB_OK;
+}
+
+bool pair_pass_sampleable(const PairParams& pp) { return pp.use_table || pp.eps2 == 0.f; }
 
 int slot_counter_words() { return SLOT_COUNTER_WORDS; }
 
@@ -696,7 +721,8 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
                 int nitems_max, u32* heavy, u32* counter, const PairParams& pp, const float* table,
                 const StepParams& sp, float kick, int drift, int kdk, float4* pm_out, float4* vi_out,
                 float4* acc_out, unsigned long long* npairs, int* stop, int num_sms, cudaEvent_t ev_pair,
-                cudaStream_t st, int equal_mass, float4* slots, int n) {
+                cudaStream_t st, int equal_mass, float4* slots, int n, int unit_stride) {
+  const u32 ustride = unit_stride > 1 ? (u32)unit_stride : 1u;
   const int ncells = chd.Mx * chd.My * chd.Mz;
   const int ntot = ncells * chd.sub * chd.sub + 1;  // sub-columns + the bucket outside the mesh
   // the slotted pass: the table, or the exact table-free force without softening
@@ -713,9 +739,10 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
   const u32 heavy_cap = (u32)slot_heavy_capacity(nitems_max);
   if (slotted && nitems_max > 0) {
     const int pb = (nitems_max + 255) / 256;
-    plan_cost_kernel<<<pb, 256, 0, st>>>(cell_start, items, nitems, cd, counter, stop);
+    plan_cost_kernel<<<pb, 256, 0, st>>>(cell_start, items, nitems, cd, counter, ustride, stop);
     plan_heavy_kernel<<<pb, 256, 0, st>>>(cell_start, items, nitems, cd, heavy, heavy_cap, counter,
-                                          (unsigned long long)num_sms * SLOT_CTAS_PER_SM * SLOT_WARPS, stop);
+                                          (unsigned long long)num_sms * SLOT_CTAS_PER_SM * SLOT_WARPS, ustride,
+                                          stop);
   }
   if (ev_pair) PMGB_CUDA_TRY(cudaEventRecord(ev_pair, st));
   const dim3 grid(num_sms * 8), block(PAIR_THREADS);
@@ -733,7 +760,7 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
     auto kern = equal_mass ? (exact ? pair_slot_kernel<true, true> : pair_slot_kernel<true, false>)
                            : (exact ? pair_slot_kernel<false, true> : pair_slot_kernel<false, false>);
     kern<<<num_sms * SLOT_CTAS_PER_SM, SLOT_THREADS, SLOT_SMEM, st>>>(
-        pm, n, cell_start, items, nitems, heavy, heavy_cap, counter, cd, pp, table, slots, stop);
+        pm, n, cell_start, items, nitems, heavy, heavy_cap, counter, cd, pp, table, slots, ustride, stop);
     if (n > 0)
       pair_epilogue_kernel<<<(n + 255) / 256, 256, 0, st>>>(pm, vi, acc_pm, slots, n, sp, kick, drift,
                                                             kdk, pm_out, vi_out, acc_out, stop);

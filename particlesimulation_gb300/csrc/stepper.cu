@@ -159,6 +159,7 @@ extern "C" int pmgb_pm_leapfrog(pmgb_pm* h, int op, float dt) {
     PMGB_CUDA_TRY(cudaMalloc(&h->ivel, sizeof(float4) * (size_t)h->n));
     PMGB_CUDA_TRY(cudaMemsetAsync(h->ivel, 0, sizeof(float4) * (size_t)h->n, h->st));
   }
+  if (op == PMGB_LEAPFROG_DRIFT) h->acc_mode = -1;  // accelerations of the old positions
   leapfrog_handle_kernel<<<(h->n + 255) / 256, 256, 0, h->st>>>(op, h->n, h->pm[h->cur], h->vi[h->cur],
                                                                 h->acc, h->ivel, dt);
   PMGB_LAUNCH_CHECK();
