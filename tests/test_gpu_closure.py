@@ -139,6 +139,35 @@ def test_closure_reproduces_plain_p3m_at_equal_direct_sum_error(gpu_lib):
     pm.close()
 
 
+def test_sampled_judge(gpu_lib):
+    """The judge's sampled full-cutoff pass (every 16th slice) against the median over all
+    particles from full force evaluations in both modes, and its reuse of the last learned
+    step's accelerations against a fresh evaluation (bit-identical: the same positions give
+    the same forces)."""
+    w = _small_disk(n=32768, seed=5, table=0)
+    pm, cl = _closure(w, capacity=w.n, seed=2)
+    pm.run(0)
+    cl.collect()
+    cl.train(epochs=5, batch=1024, lr=2e-3)
+    cl.setMode(cl.LEARNED)
+    pm.advance(1)  # a learned step: the judge reuses its accelerations
+    j_reused = cl.judge(stride=16)
+    x, v, _ = pm.getParticles(units="code")
+    pm.setParticles(x, v, units="code")  # same state, stored accelerations no longer current
+    j_fresh = cl.judge(stride=16)
+    assert j_reused == j_fresh
+    acc = {}
+    for mode in (cl.FULL, cl.LEARNED):
+        cl.setMode(mode)
+        cl.force()
+        acc[mode] = pm.getParticles()[2].astype(np.float64)
+    d = np.linalg.norm(acc[cl.LEARNED] - acc[cl.FULL], axis=1) / np.linalg.norm(acc[cl.FULL], axis=1)
+    full_median = float(np.median(d))
+    assert 0.7 * full_median < j_fresh < 1.4 * full_median, (j_fresh, full_median)
+    cl.close()
+    pm.close()
+
+
 def test_judge_falls_back_to_plain_p3m(gpu_lib):
     """With a bound no closure can meet, the judged run switches to plain P3M at its first
     check and then matches a plain-P3M run."""
