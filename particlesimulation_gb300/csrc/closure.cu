@@ -11,9 +11,9 @@
 //                 units (3)
 //   network       67 -> 64 -> 64 -> 64 -> 3, GELU, BF16 weights and activations, FP32
 //                 accumulation.  Inference: tcgen05.mma from shared memory into TMEM, 128
-//                 particles per CTA (the tcgen05 forward below).  Training (forward, backward):
-//                 mma.sync m16n8k16 tiles, one warp per 16 rows, layer outputs kept in
-//                 registers as the next layer's operands
+//                 particles per CTA (the tcgen05 forward below).  Training (forward,
+//                 backward): tcgen05.mma too, 128 rows per CTA, pre-activations kept in TMEM
+//                 and the weight gradients as M = 128 products over the batch tile
 //   output  (3)   residual / (S * c), c = 1 / (4 pi HC'^2)  (the residual is linear in the
 //                 masses, so scaling by S makes the map scale free)
 // Training pairs are the exact residual from the plain P3M itself (full-cutoff force minus
@@ -40,29 +40,17 @@ constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + CL_H * CL_K0, OFF_W2 = OFF_B1 + CL_H
               OFF_B2 = OFF_W2 + CL_H * CL_H, OFF_W3 = OFF_B2 + CL_H,
               OFF_B3 = OFF_W3 + CL_H * CL_H, OFF_W4 = OFF_B3 + CL_H,
               OFF_B4 = OFF_W4 + CL_NO * CL_H, CL_NPARAM = OFF_B4 + CL_NO;
-// bf16 weight image in shared memory, row strides padded against bank conflicts
-constexpr int S80 = 88, S64 = 72, S16 = 24;
+// BF16 image of the weights (rows out x in, padded strides) and of the transposes the backward
+// pass multiplies by; the kernels copy it into their canonical shared-memory operands
+constexpr int S80 = 88, S64 = 72;
 constexpr int IMG_W1 = 0, IMG_W2 = IMG_W1 + CL_H * S80, IMG_W3 = IMG_W2 + CL_H * S64,
               IMG_W4 = IMG_W3 + CL_H * S64, IMG_W2T = IMG_W4 + CL_NO * S64,
-              IMG_W3T = IMG_W2T + CL_H * S64, IMG_W4T = IMG_W3T + CL_H * S64,
-              IMG_SIZE = IMG_W4T + CL_H * S16;  // bf16 elements
-constexpr int CL_WARPS = 4, CL_THREADS = CL_WARPS * 32;
+              IMG_W3T = IMG_W2T + CL_H * S64, IMG_SIZE = IMG_W3T + CL_H * S64;  // bf16 elements
 
 // ------------------------------------------------------------------ helpers -----------
-__device__ __forceinline__ u32 ld32(const bf16* p) { return *reinterpret_cast<const u32*>(p); }
 __device__ __forceinline__ u32 pack_bf16(float lo, float hi) {
   __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
   return *reinterpret_cast<u32*>(&v);
-}
-__device__ __forceinline__ u32 pack_raw(bf16 lo, bf16 hi) {
-  return (u32)__bfloat16_as_ushort(lo) | ((u32)__bfloat16_as_ushort(hi) << 16);
-}
-__device__ __forceinline__ void mma16816(float c[4], const u32 a[4], const u32 b[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-      "{%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 __device__ __forceinline__ float gelu(float x) {
   return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f));
@@ -70,104 +58,6 @@ __device__ __forceinline__ float gelu(float x) {
 __device__ __forceinline__ float gelu_grad(float x) {
   return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) +
          x * 0.39894228040143268f * expf(-0.5f * x * x);
-}
-
-// Fragments of m16n8k16 (g = lane / 4, t = lane % 4):
-//   A (16x16, row-major): a0 (g, 2t..2t+1), a1 (g+8, 2t..), a2 (g, 2t+8..), a3 (g+8, 2t+8..)
-//   B (16x8, k x n):      b0 (k = 2t..2t+1, n = g), b1 (k = 2t+8.., n = g)
-//   C (16x8):             c0, c1 (g, 2t..2t+1), c2, c3 (g+8, 2t..2t+1)
-// A[r][k] = M[r0 + r][k0 + k], M row-major with stride S
-__device__ __forceinline__ void ld_a(u32 a[4], const bf16* M, int S, int r0, int k0, int g, int t) {
-  a[0] = ld32(M + (r0 + g) * S + k0 + 2 * t);
-  a[1] = ld32(M + (r0 + g + 8) * S + k0 + 2 * t);
-  a[2] = ld32(M + (r0 + g) * S + k0 + 8 + 2 * t);
-  a[3] = ld32(M + (r0 + g + 8) * S + k0 + 8 + 2 * t);
-}
-// A[r][k] = M[k0 + k][r0 + r]
-__device__ __forceinline__ void ld_a_t(u32 a[4], const bf16* M, int S, int r0, int k0, int g, int t) {
-  a[0] = pack_raw(M[(k0 + 2 * t) * S + r0 + g], M[(k0 + 2 * t + 1) * S + r0 + g]);
-  a[1] = pack_raw(M[(k0 + 2 * t) * S + r0 + g + 8], M[(k0 + 2 * t + 1) * S + r0 + g + 8]);
-  a[2] = pack_raw(M[(k0 + 2 * t + 8) * S + r0 + g], M[(k0 + 2 * t + 9) * S + r0 + g]);
-  a[3] = pack_raw(M[(k0 + 2 * t + 8) * S + r0 + g + 8], M[(k0 + 2 * t + 9) * S + r0 + g + 8]);
-}
-// B[k][n] = W[n0 + n][k0 + k], W row-major with stride S (a weight matrix stored out x in)
-__device__ __forceinline__ void ld_b(u32 b[2], const bf16* W, int S, int n0, int k0, int g, int t) {
-  b[0] = ld32(W + (n0 + g) * S + k0 + 2 * t);
-  b[1] = ld32(W + (n0 + g) * S + k0 + 8 + 2 * t);
-}
-// B[k][n] = M[k0 + k][n0 + n]
-__device__ __forceinline__ void ld_b_rm(u32 b[2], const bf16* M, int S, int n0, int k0, int g, int t) {
-  b[0] = pack_raw(M[(k0 + 2 * t) * S + n0 + g], M[(k0 + 2 * t + 1) * S + n0 + g]);
-  b[1] = pack_raw(M[(k0 + 2 * t + 8) * S + n0 + g], M[(k0 + 2 * t + 9) * S + n0 + g]);
-}
-
-// One dense layer for a warp's 16 rows: out[nt] (C fragments, NT tiles of 8 columns) =
-// A (KS k-slices of 16) x W^T + bias.
-template <int NT, int KS>
-__device__ __forceinline__ void dense(float out[NT][4], const u32 a[KS][4], const bf16* W, int S,
-                                      const float* bias, int g, int t) {
-#pragma unroll
-  for (int nt = 0; nt < NT; ++nt) {
-    const float b0 = bias[nt * 8 + 2 * t], b1 = bias[nt * 8 + 2 * t + 1];
-    out[nt][0] = b0;
-    out[nt][1] = b1;
-    out[nt][2] = b0;
-    out[nt][3] = b1;
-#pragma unroll
-    for (int ks = 0; ks < KS; ++ks) {
-      u32 b[2];
-      ld_b(b, W, S, nt * 8, ks * 16, g, t);
-      mma16816(out[nt], a[ks], b);
-    }
-  }
-}
-
-// GELU of 8 C tiles (16 x 64) into 4 A k-slices (register-only chaining).
-__device__ __forceinline__ void act_to_a(u32 a[4][4], const float z[8][4]) {
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    a[j][0] = pack_bf16(gelu(z[2 * j][0]), gelu(z[2 * j][1]));
-    a[j][1] = pack_bf16(gelu(z[2 * j][2]), gelu(z[2 * j][3]));
-    a[j][2] = pack_bf16(gelu(z[2 * j + 1][0]), gelu(z[2 * j + 1][1]));
-    a[j][3] = pack_bf16(gelu(z[2 * j + 1][2]), gelu(z[2 * j + 1][3]));
-  }
-}
-
-struct SmemMLP {
-  bf16 img[IMG_SIZE];
-  float bias[CL_H * 3 + CL_NO];  // b1, b2, b3, b4
-};
-
-__device__ void load_mlp_smem(SmemMLP& s, const bf16* __restrict__ img, const float* __restrict__ p) {
-  const u32* src = reinterpret_cast<const u32*>(img);
-  u32* dst = reinterpret_cast<u32*>(s.img);
-  for (int i = threadIdx.x; i < IMG_SIZE / 2; i += blockDim.x) dst[i] = src[i];
-  for (int i = threadIdx.x; i < CL_H; i += blockDim.x) {
-    s.bias[i] = p[OFF_B1 + i];
-    s.bias[CL_H + i] = p[OFF_B2 + i];
-    s.bias[2 * CL_H + i] = p[OFF_B3 + i];
-  }
-  for (int i = threadIdx.x; i < CL_NO; i += blockDim.x) s.bias[3 * CL_H + i] = p[OFF_B4 + i];
-}
-
-// Forward pass of a warp's 16 rows held as A fragments x0 (5 k-slices); returns the output tile
-// and, for training, the pre-activations.
-template <bool KEEP>
-__device__ __forceinline__ void mlp_forward(const SmemMLP& s, const u32 x0[5][4], float y[4],
-                                            float z1[8][4], float z2[8][4], float z3[8][4],
-                                            u32 a1[4][4], u32 a2[4][4], u32 a3[4][4], int g, int t) {
-  dense<8, 5>(z1, x0, s.img + IMG_W1, S80, s.bias, g, t);
-  act_to_a(a1, z1);
-  dense<8, 4>(z2, a1, s.img + IMG_W2, S64, s.bias + CL_H, g, t);
-  act_to_a(a2, z2);
-  dense<8, 4>(z3, a2, s.img + IMG_W3, S64, s.bias + 2 * CL_H, g, t);
-  act_to_a(a3, z3);
-  float out[1][4];
-  dense<1, 4>(out, a3, s.img + IMG_W4, S64, s.bias + 3 * CL_H, g, t);
-  y[0] = out[0][0];
-  y[1] = out[0][1];
-  y[2] = out[0][2];
-  y[3] = out[0][3];
 }
 
 // ------------------------------------------------------------------ occupancy --------
@@ -262,7 +152,6 @@ __device__ __forceinline__ float features(const ReducedMesh& rm, const float* __
 // bounded (1 s of %globaltimer, and a poll count); a wait that gives up sets err[0], the thread
 // waits no more and thread 0 issues no more MMAs, while the barriers stay where they are, so
 // the kernel reaches its end (and frees its TMEM) and the host reports PMGB_ETIMEOUT.
-// Training keeps the mma.sync kernels above.
 constexpr int TC_ROWS = 128;
 constexpr int TC_THREADS = 128;
 constexpr int TC_N4 = 16;                   // output layer, padded
@@ -305,10 +194,9 @@ __host__ __device__ constexpr u32 tc_idesc(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((u32)(N >> 3) << 17) | ((u32)(M >> 4) << 24);
 }
 
-// D (TMEM) = A x B^T over nks K slices of 16, then a commit to the mbarrier (one thread)
-__device__ __forceinline__ void tc_mma_layer(u32 tmem, u32 a, u32 akstride, u32 b, u32 bkstride,
-                                             int nks, u32 idesc, u32 mbar) {
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+// D (TMEM) = A x B^T over nks K slices of 16 (one thread; no fence, no commit)
+__device__ __forceinline__ void tc_mmas(u32 tmem, u32 a, u32 akstride, u32 b, u32 bkstride, int nks,
+                                        u32 idesc) {
   for (int ks = 0; ks < nks; ++ks) {
     const u64 ad = tc_desc(a + 2u * ks * akstride, akstride);
     const u64 bd = tc_desc(b + 2u * ks * bkstride, bkstride);
@@ -317,8 +205,20 @@ __device__ __forceinline__ void tc_mma_layer(u32 tmem, u32 a, u32 akstride, u32 
         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
         :: "r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(ks > 0 ? 1u : 0u) : "memory");
   }
+}
+
+// the mbarrier completes a phase once every MMA this thread issued so far has finished
+__device__ __forceinline__ void tc_commit(u32 mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                :: "r"(mbar) : "memory");
+}
+
+// D (TMEM) = A x B^T over nks K slices of 16, then a commit to the mbarrier (one thread)
+__device__ __forceinline__ void tc_mma_layer(u32 tmem, u32 a, u32 akstride, u32 b, u32 bkstride,
+                                             int nks, u32 idesc, u32 mbar) {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  tc_mmas(tmem, a, akstride, b, bkstride, nks, idesc);
+  tc_commit(mbar);
 }
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
@@ -485,13 +385,15 @@ __device__ __forceinline__ void tc_forward(TcSmem& s, u32& phase, bool& live, in
   __syncthreads();
 }
 
-__device__ __forceinline__ void tc_teardown(TcSmem& s) {
+// Epilogue of a CTA: every thread is past its TMEM reads, warp 0 frees the columns.
+__device__ __forceinline__ void tc_free(u32 tmem, u32 cols) {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (threadIdx.x < 32)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(s.tmem), "r"(TC_COLS) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(cols) : "memory");
 }
+__device__ __forceinline__ void tc_teardown(TcSmem& s) { tc_free(s.tmem, TC_COLS); }
 
 // ------------------------------------------------------------------ inference --------
 // acc[i] += MLP(features(i)) * S * c, for the particles of this handle (sorted order).
@@ -534,192 +436,277 @@ __global__ void __launch_bounds__(TC_THREADS) closure_infer_kernel(
 }
 
 // ------------------------------------------------------------------ training ---------
-// Per warp: 16 training rows (by permutation), forward, loss, backward; per-warp partial
-// gradients go to gw[warp][CL_NPARAM] (reduced deterministically by grad_reduce_kernel).
-struct TrainSmemWarp {
-  bf16 x[16 * S80];
-  bf16 a1[16 * S64], a2[16 * S64], a3[16 * S64];
-  bf16 d[16 * S64];
-  bf16 dy[16 * S16];
+// Training runs on the tensor cores too: one CTA of 128 threads per 128 training rows (thread
+// r = row r = TMEM lane r), every MMA with M = 128.  The forward pass is the inference one,
+// except that each layer's pre-activations stay in their own TMEM columns (the backward pass
+// reads them for GELU') and each layer's BF16 activations are also stored transposed (rows =
+// features, K = the 128 rows of the batch tile) as the B operand of the next weight gradient.
+// Backward, for layer l with input activations A (the features x for l = 1):
+//   dW_l  (rows j = the layer's outputs, N = 80) = dZ_l^T (rows j, K = rows b) x A^T (rows i,
+//         K = b).  Row 64 of the hidden A^T operands (row 67 of the input's) is all ones, so
+//         column 64 (67) of the product is the bias gradient sum_b dZ_l[b][j]; rows j >= 64 of
+//         dZ^T are zero and their products are not read
+//   dA    (rows b, N = 64) = dZ_l (rows b, K = j) x W_l, the B operand being W_l^T (rows i,
+//         K = j)
+// and dZ = dA * GELU'(Z) per row in FP32, stored in BF16 both ways.  The output layer's dY (16
+// columns, 3 non-zero) stands in for dZ_4.  TMEM columns (512 allocated):
+//   Z1 0, Z2 64, Z3 128, Y 192 | dW4 256, dA3 336 | dW3 400, dA2 192 | dW2 256, dA1 336 | dW1 400
+// (each region is reused only after every thread has read what it held).  The CTA's partial
+// gradient goes to gw[cta][CL_NPARAM] and its loss to lossw[cta]; grad_reduce_kernel sums them
+// in a fixed order.  Waits are bounded as in the inference kernel (err[0] on a timeout).
+constexpr int TT_N = 80;                 // rows of the transposed activation operands
+constexpr u32 TT_K = TT_N * 16;          // their K-group stride (K = the batch tile's rows)
+constexpr u32 TD_K = TC_ROWS * 16;       // K-group stride of dZ^T (128 rows)
+constexpr u32 TT_COLS = 512;
+
+struct TcTrainSmem {
+  alignas(16) bf16 w1[CL_H * CL_K0];
+  alignas(16) bf16 w2[CL_H * CL_H];
+  alignas(16) bf16 w3[CL_H * CL_H];
+  alignas(16) bf16 w4[TC_N4 * CL_H];
+  alignas(16) bf16 w2t[CL_H * CL_H];        // rows i, K = j: W2[j][i]
+  alignas(16) bf16 w3t[CL_H * CL_H];
+  alignas(16) bf16 w4t[CL_H * TC_N4];       // rows j, K = o: W4[o][j] (zero for o >= 8)
+  alignas(16) bf16 x[TC_ROWS * CL_K0];      // rows b, K = input features
+  alignas(16) bf16 h[TC_ROWS * CL_H];       // rows b, K = j: activations, then dZ
+  alignas(16) bf16 dy[TC_ROWS * TC_N4];     // rows b, K = o
+  alignas(16) bf16 xt[TT_N * TC_ROWS];      // rows = input features (ones at 67), K = b
+  alignas(16) bf16 at[3][TT_N * TC_ROWS];   // rows = hidden features (ones at 64), K = b
+  alignas(16) bf16 dzt[TC_ROWS * TC_ROWS];  // rows j (dY^T in rows 0..15, then dZ^T), K = b
+  float bias[3 * CL_H + TC_N4];
+  float lsum[TC_THREADS / 32];
+  u64 mbar;
+  u32 tmem;
 };
 
-__global__ void __launch_bounds__(CL_THREADS) closure_train_kernel(
-    const bf16* __restrict__ X, const float* __restrict__ T, const int* __restrict__ perm,
-    int batch_off, int batch, float inv_batch, const bf16* __restrict__ img,
-    const float* __restrict__ params, float* __restrict__ gw, float* __restrict__ lossw) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemMLP& s = *reinterpret_cast<SmemMLP*>(smem_raw);
-  TrainSmemWarp* tw_all = reinterpret_cast<TrainSmemWarp*>(smem_raw + sizeof(SmemMLP));
-  load_mlp_smem(s, img, params);
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  TrainSmemWarp& w = tw_all[warp];
-  const int gwarp = blockIdx.x * CL_WARPS + warp;
-  const int r0 = gwarp * 16;
-  float* G = gw + (size_t)gwarp * CL_NPARAM;
-  // stage inputs
-  for (int e = lane; e < 16 * (CL_K0 / 2); e += 32) {
-    const int r = e / (CL_K0 / 2), c2 = e % (CL_K0 / 2);
-    const int row = r0 + r;
-    u32 v = 0u;
-    if (row < batch) v = reinterpret_cast<const u32*>(X + (size_t)perm[batch_off + row] * CL_K0)[c2];
-    *reinterpret_cast<u32*>(w.x + r * S80 + 2 * c2) = v;
-  }
-  __syncwarp();
-  u32 x0[5][4];
+// column b of a canonical operand whose K dimension is the batch row: rows 0..n-1 from v
+template <int N>
+__device__ __forceinline__ void tc_store_col(bf16* base, int b, u32 kstride, const float* v) {
+  unsigned char* p = reinterpret_cast<unsigned char*>(base);
 #pragma unroll
-  for (int ks = 0; ks < 5; ++ks) ld_a(x0[ks], w.x, S80, 0, ks * 16, g, t);
-  float y[4], z1[8][4], z2[8][4], z3[8][4];
-  u32 a1[4][4], a2[4][4], a3[4][4];
-  mlp_forward<true>(s, x0, y, z1, z2, z3, a1, a2, a3, g, t);
-  // activations to shared memory (for the weight gradients)
-  auto store_act = [&](bf16* dst, const u32 a[4][4]) {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      *reinterpret_cast<u32*>(dst + g * S64 + 16 * j + 2 * t) = a[j][0];
-      *reinterpret_cast<u32*>(dst + (g + 8) * S64 + 16 * j + 2 * t) = a[j][1];
-      *reinterpret_cast<u32*>(dst + g * S64 + 16 * j + 8 + 2 * t) = a[j][2];
-      *reinterpret_cast<u32*>(dst + (g + 8) * S64 + 16 * j + 8 + 2 * t) = a[j][3];
-    }
-  };
-  store_act(w.a1, a1);
-  store_act(w.a2, a2);
-  store_act(w.a3, a3);
-  // dY and loss
-  float loss = 0.f;
-  float dy[4];
-#pragma unroll
-  for (int e = 0; e < 4; ++e) {
-    const int r = g + 8 * (e >> 1), o = 2 * t + (e & 1), row = r0 + r;
-    float d = 0.f;
-    if (row < batch && o < 3) {
-      const float diff = y[e] - T[(size_t)perm[batch_off + row] * 4 + o];
-      loss += diff * diff;
-      d = 2.0f * diff * inv_batch;
-    }
-    dy[e] = d;
-  }
-  for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xFFFFFFFFu, loss, o);
-  if (lane == 0) lossw[gwarp] = loss;
-  // dY tile (16 x 16, columns 8..15 zero)
-  *reinterpret_cast<u32*>(w.dy + g * S16 + 2 * t) = pack_bf16(dy[0], dy[1]);
-  *reinterpret_cast<u32*>(w.dy + (g + 8) * S16 + 2 * t) = pack_bf16(dy[2], dy[3]);
-  *reinterpret_cast<u32*>(w.dy + g * S16 + 8 + 2 * t) = 0u;
-  *reinterpret_cast<u32*>(w.dy + (g + 8) * S16 + 8 + 2 * t) = 0u;
-  __syncwarp();
-
-  // bias gradient of a C-tile column pair: sum over rows g, g+8 and over g
-  auto col_sums = [&](float c0, float c1, float& s0, float& s1) {
-    s0 = c0;
-    s1 = c1;
-    for (int o = 4; o < 32; o <<= 1) {
-      s0 += __shfl_xor_sync(0xFFFFFFFFu, s0, o);
-      s1 += __shfl_xor_sync(0xFFFFFFFFu, s1, o);
-    }
-  };
-  // ---- layer 4: dW4 = dY^T A3 (16 padded outputs x 64), db4, dA3 = dY W4
-  {
-    u32 aT[4];
-    ld_a_t(aT, w.dy, S16, 0, 0, g, t);  // A[o][b] = dY[b][o]
-#pragma unroll
-    for (int nt = 0; nt < 8; ++nt) {
-      float c[4] = {0.f, 0.f, 0.f, 0.f};
-      u32 b[2];
-      ld_b_rm(b, w.a3, S64, nt * 8, 0, g, t);  // B[b][j] = A3[b][j]
-      mma16816(c, aT, b);
-      if (g < CL_NO) {
-        G[OFF_W4 + g * CL_H + nt * 8 + 2 * t] = c[0];
-        G[OFF_W4 + g * CL_H + nt * 8 + 2 * t + 1] = c[1];
-      }
-    }
-    float s0, s1;
-    col_sums(dy[0] + dy[2], dy[1] + dy[3], s0, s1);
-    if (g == 0) {
-      G[OFF_B4 + 2 * t] = s0;
-      G[OFF_B4 + 2 * t + 1] = s1;
-    }
-  }
-  float dz[8][4];
-  {
-    u32 ad[4];
-    ld_a(ad, w.dy, S16, 0, 0, g, t);
-#pragma unroll
-    for (int nt = 0; nt < 8; ++nt) {
-      dz[nt][0] = dz[nt][1] = dz[nt][2] = dz[nt][3] = 0.f;
-      u32 b[2];
-      ld_b(b, s.img + IMG_W4T, S16, nt * 8, 0, g, t);  // B[o][j] = W4[o][j] = W4T[j][o]
-      mma16816(dz[nt], ad, b);
-    }
-  }
-  // ---- hidden layers 3, 2, 1
-  auto hidden_backward = [&](float z[8][4], const bf16* a_in, int a_stride, int kin, int off_w,
-                             int off_b, const bf16* wt, bool need_dx) {
-    // dZ = dA * gelu'(Z)  (in place in dz), bias gradient, dZ to shared memory
-#pragma unroll
-    for (int nt = 0; nt < 8; ++nt) {
-#pragma unroll
-      for (int e = 0; e < 4; ++e) dz[nt][e] *= gelu_grad(z[nt][e]);
-      float s0, s1;
-      col_sums(dz[nt][0] + dz[nt][2], dz[nt][1] + dz[nt][3], s0, s1);
-      if (g == 0) {
-        G[off_b + nt * 8 + 2 * t] = s0;
-        G[off_b + nt * 8 + 2 * t + 1] = s1;
-      }
-      *reinterpret_cast<u32*>(w.d + g * S64 + nt * 8 + 2 * t) = pack_bf16(dz[nt][0], dz[nt][1]);
-      *reinterpret_cast<u32*>(w.d + (g + 8) * S64 + nt * 8 + 2 * t) = pack_bf16(dz[nt][2], dz[nt][3]);
-    }
-    __syncwarp();
-    // dW[j][i] = sum_b dZ[b][j] A_in[b][i]: 4 m-tiles (j) x kin/8 n-tiles (i), K = 16 rows
-#pragma unroll
-    for (int mt = 0; mt < 4; ++mt) {
-      u32 aT[4];
-      ld_a_t(aT, w.d, S64, mt * 16, 0, g, t);
-      for (int nt = 0; nt < kin / 8; ++nt) {
-        float c[4] = {0.f, 0.f, 0.f, 0.f};
-        u32 b[2];
-        ld_b_rm(b, a_in, a_stride, nt * 8, 0, g, t);
-        mma16816(c, aT, b);
-        const int j0 = mt * 16 + g, i0 = nt * 8 + 2 * t;
-        G[off_w + j0 * kin + i0] = c[0];
-        G[off_w + j0 * kin + i0 + 1] = c[1];
-        G[off_w + (j0 + 8) * kin + i0] = c[2];
-        G[off_w + (j0 + 8) * kin + i0 + 1] = c[3];
-      }
-    }
-    if (need_dx) {
-      // dA_in = dZ W  (W stored out x in; B[j][i] = W[j][i] = WT[i][j])
-      u32 ad[4][4];
-#pragma unroll
-      for (int ks = 0; ks < 4; ++ks) ld_a(ad[ks], w.d, S64, 0, ks * 16, g, t);
-#pragma unroll
-      for (int nt = 0; nt < 8; ++nt) {
-        dz[nt][0] = dz[nt][1] = dz[nt][2] = dz[nt][3] = 0.f;
-#pragma unroll
-        for (int ks = 0; ks < 4; ++ks) {
-          u32 b[2];
-          ld_b(b, wt, S64, nt * 8, ks * 16, g, t);
-          mma16816(dz[nt], ad[ks], b);
-        }
-      }
-    }
-    __syncwarp();
-  };
-  hidden_backward(z3, w.a2, S64, CL_H, OFF_W3, OFF_B3, s.img + IMG_W3T, true);
-  hidden_backward(z2, w.a1, S64, CL_H, OFF_W2, OFF_B2, s.img + IMG_W2T, true);
-  hidden_backward(z1, w.x, S80, CL_K0, OFF_W1, OFF_B1, nullptr, false);
+  for (int r = 0; r < N; ++r) *reinterpret_cast<bf16*>(p + canon(r, b, kstride)) = __float2bfloat16_rn(v[r]);
 }
 
-__global__ void grad_reduce_kernel(const float* __restrict__ gw, int nwarps, float* __restrict__ grad,
+__device__ __forceinline__ void tc_put(bf16* base, int r, int k, u32 kstride, bf16 v) {
+  *reinterpret_cast<bf16*>(reinterpret_cast<unsigned char*>(base) + canon(r, k, kstride)) = v;
+}
+
+__global__ void __launch_bounds__(TC_THREADS) closure_train_kernel(
+    const bf16* __restrict__ X, const float* __restrict__ T, const int* __restrict__ perm,
+    int batch_off, int batch, float inv_batch, const bf16* __restrict__ img,
+    const float* __restrict__ params, float* __restrict__ gw, float* __restrict__ lossw,
+    int* __restrict__ err) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TcTrainSmem& s = *reinterpret_cast<TcTrainSmem*>(smem_raw);
+  const int tid = threadIdx.x;
+  const bf16 zero = __float2bfloat16_rn(0.f), one = __float2bfloat16_rn(1.f);
+  // weights, their transposes, biases; the constant rows of the transposed operands
+  for (int e = tid; e < CL_H * CL_K0; e += TC_THREADS)
+    tc_put(s.w1, e / CL_K0, e % CL_K0, TC_KW, img[IMG_W1 + (e / CL_K0) * S80 + e % CL_K0]);
+  for (int e = tid; e < CL_H * CL_H; e += TC_THREADS) {
+    const int n = e / CL_H, k = e % CL_H;
+    tc_put(s.w2, n, k, TC_KW, img[IMG_W2 + n * S64 + k]);
+    tc_put(s.w3, n, k, TC_KW, img[IMG_W3 + n * S64 + k]);
+    tc_put(s.w2t, n, k, TC_KW, img[IMG_W2T + n * S64 + k]);
+    tc_put(s.w3t, n, k, TC_KW, img[IMG_W3T + n * S64 + k]);
+  }
+  for (int e = tid; e < TC_N4 * CL_H; e += TC_THREADS) {
+    const int o = e / CL_H, j = e % CL_H;
+    const bf16 v = o < CL_NO ? img[IMG_W4 + o * S64 + j] : zero;
+    tc_put(s.w4, o, j, TC_KW4, v);
+    tc_put(s.w4t, j, o, TC_KW, v);
+  }
+  for (int i = tid; i < CL_H; i += TC_THREADS) {
+    s.bias[i] = params[OFF_B1 + i];
+    s.bias[CL_H + i] = params[OFF_B2 + i];
+    s.bias[2 * CL_H + i] = params[OFF_B3 + i];
+  }
+  for (int i = tid; i < TC_N4; i += TC_THREADS) s.bias[3 * CL_H + i] = i < CL_NO ? params[OFF_B4 + i] : 0.f;
+  for (int e = tid; e < (TT_N - CL_IN) * TC_ROWS; e += TC_THREADS) {
+    const int r = CL_IN + e / TC_ROWS;
+    tc_put(s.xt, r, e % TC_ROWS, TT_K, r == CL_IN ? one : zero);
+  }
+  for (int e = tid; e < (TT_N - CL_H) * TC_ROWS; e += TC_THREADS) {
+    const int r = CL_H + e / TC_ROWS;
+#pragma unroll
+    for (int l = 0; l < 3; ++l) tc_put(s.at[l], r, e % TC_ROWS, TT_K, r == CL_H ? one : zero);
+  }
+  for (int e = tid; e < TC_ROWS * TC_ROWS / 8; e += TC_THREADS)
+    reinterpret_cast<uint4*>(s.dzt)[e] = make_uint4(0u, 0u, 0u, 0u);
+  if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(&s.mbar)) : "memory");
+  if (tid < 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 :: "r"(smem_addr(&s.tmem)), "r"(TT_COLS) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  // this thread's training row: BF16 features to x (rows b) and xt (column b)
+  const int row = blockIdx.x * TC_ROWS + tid;
+  const bool valid = row < batch;
+  const int src = valid ? perm[batch_off + row] : 0;
+  {
+    float f[CL_K0];
+    const uint4* xr = reinterpret_cast<const uint4*>(X + (size_t)src * CL_K0);
+#pragma unroll
+    for (int j = 0; j < CL_K0 / 8; ++j) {
+      const uint4 q = valid ? xr[j] : make_uint4(0u, 0u, 0u, 0u);
+      *reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(s.x) + canon(tid, 8 * j, TC_KX)) = q;
+      const u32 w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+      for (int h = 0; h < 4; ++h) {
+        f[8 * j + 2 * h] = __uint_as_float(w[h] << 16);
+        f[8 * j + 2 * h + 1] = __uint_as_float(w[h] & 0xFFFF0000u);
+      }
+    }
+    tc_store_col<CL_IN>(s.xt, tid, TT_K, f);
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+  const u32 tmem = s.tmem;
+  const u32 lane = tmem + ((u32)(tid & ~31) << 16);
+  const u32 mbar = smem_addr(&s.mbar);
+  const u32 xa = smem_addr(s.x), ha = smem_addr(s.h), dya = smem_addr(s.dy), dzta = smem_addr(s.dzt);
+  const u32 xta = smem_addr(s.xt);
+  const u32 ata[3] = {smem_addr(s.at[0]), smem_addr(s.at[1]), smem_addr(s.at[2])};
+  const u32 wa[3] = {smem_addr(s.w1), smem_addr(s.w2), smem_addr(s.w3)};
+  const bool issuer = tid == 0;
+  u32 phase = 0;
+  bool live = true;
+  auto wait = [&]() {
+    if (live && !tc_wait(mbar, phase & 1u)) {
+      live = false;
+      atomicExch(err, 1);
+    }
+    ++phase;
+  };
+  // shared-memory operands written by every thread, TMEM reads done: next MMAs may start
+  auto publish = [&]() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+  };
+  float* G = gw + (size_t)blockIdx.x * CL_NPARAM;
+
+  // ---- forward: Z_l into TMEM columns 64 l, activations to h (rows b) and at[l] (column b)
+  constexpr u32 colZ[3] = {0u, 64u, 128u};
+#pragma unroll 1
+  for (int l = 0; l < 3; ++l) {
+    if (issuer && live) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      tc_mmas(tmem + colZ[l], l == 0 ? xa : ha, TC_KX, wa[l], TC_KW, l == 0 ? CL_K0 / 16 : CL_H / 16,
+              tc_idesc(TC_ROWS, CL_H));
+      tc_commit(mbar);
+    }
+    wait();
+    float z[64];
+    tc_ld64(lane + colZ[l], z);
+    const float* b = s.bias + l * CL_H;
+#pragma unroll
+    for (int j = 0; j < 64; ++j) z[j] = gelu(z[j] + b[j]);
+    tc_store_row<CL_H / 8>(reinterpret_cast<unsigned char*>(s.h), tid, TC_KX, z);
+    tc_store_col<CL_H>(s.at[l], tid, TT_K, z);
+    publish();
+  }
+  if (issuer && live) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    tc_mmas(tmem + 192u, ha, TC_KX, smem_addr(s.w4), TC_KW4, CL_H / 16, tc_idesc(TC_ROWS, TC_N4));
+    tc_commit(mbar);
+  }
+  wait();
+  // ---- loss and dY = 2 (y - t) / batch
+  {
+    float o[16], dy[TC_N4];
+    tc_ld16(lane + 192u, o);
+    float loss = 0.f;
+#pragma unroll
+    for (int k = 0; k < TC_N4; ++k) dy[k] = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      if (valid) {
+        const float diff = o[k] + s.bias[3 * CL_H + k] - T[(size_t)src * 4 + k];
+        loss += diff * diff;
+        dy[k] = 2.0f * diff * inv_batch;
+      }
+    }
+    tc_store_row<TC_N4 / 8>(reinterpret_cast<unsigned char*>(s.dy), tid, TC_KX, dy);
+    tc_store_col<TC_N4>(s.dzt, tid, TD_K, dy);
+    for (int d = 16; d > 0; d >>= 1) loss += __shfl_xor_sync(0xFFFFFFFFu, loss, d);
+    if ((tid & 31) == 0) s.lsum[tid >> 5] = loss;
+  }
+  publish();
+  if (tid == 0) lossw[blockIdx.x] = (s.lsum[0] + s.lsum[1]) + (s.lsum[2] + s.lsum[3]);
+
+  // rows j < rows of the weight gradient in TMEM columns col..col+79: W (kin columns) and the
+  // bias (column bcol; a W column at bcol is the gradient of a zero input and is written 0)
+  auto store_dw = [&](u32 col, int rows, int kin, int off_w, int off_b, int bcol) {
+    if ((tid & ~31) < rows) {  // whole warps: tcgen05.ld is warp-wide
+      float a[64], c[16];
+      tc_ld64(lane + col, a);
+      tc_ld16(lane + col + 64u, c);
+      if (tid < rows) {
+        float* gr = G + off_w + (size_t)tid * kin;
+#pragma unroll
+        for (int i = 0; i < 64; ++i) gr[i] = (i == bcol) ? 0.f : a[i];
+#pragma unroll
+        for (int i = 64; i < 80; ++i)
+          if (i < kin) gr[i] = (i == bcol) ? 0.f : c[i - 64];
+        G[off_b + tid] = bcol < 64 ? a[bcol & 63] : c[(bcol - 64) & 15];
+      }
+    }
+  };
+  // dZ = dA * GELU'(Z + b) of this row, to dzt (column b) and, when `rows`, to h (row b)
+  auto make_dz = [&](u32 col_da, u32 col_z, const float* b, bool rows) {
+    float da[64], z[64];
+    tc_ld64(lane + col_da, da);
+    tc_ld64(lane + col_z, z);
+#pragma unroll
+    for (int j = 0; j < 64; ++j) da[j] *= gelu_grad(z[j] + b[j]);
+    if (rows) tc_store_row<CL_H / 8>(reinterpret_cast<unsigned char*>(s.h), tid, TC_KX, da);
+    tc_store_col<CL_H>(s.dzt, tid, TD_K, da);
+  };
+  auto issue_pair = [&](u32 col_dw, u32 bt, u32 col_da, u32 wt, int nks_da, u32 a_da, u32 akstride, u32 n_da) {
+    if (issuer && live) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      tc_mmas(tmem + col_dw, dzta, TD_K, bt, TT_K, TC_ROWS / 16, tc_idesc(TC_ROWS, TT_N));
+      if (nks_da > 0) tc_mmas(tmem + col_da, a_da, akstride, wt, TC_KW, nks_da, tc_idesc(TC_ROWS, n_da));
+      tc_commit(mbar);
+    }
+    wait();
+  };
+  // ---- output layer: dW4 (+ db4), dA3 = dY W4
+  issue_pair(256u, ata[2], 336u, smem_addr(s.w4t), TC_N4 / 16, dya, TC_KX, CL_H);
+  store_dw(256u, CL_NO, CL_H, OFF_W4, OFF_B4, CL_H);
+  make_dz(336u, colZ[2], s.bias + 2 * CL_H, true);
+  publish();
+  // ---- layer 3: dW3 (+ db3), dA2 = dZ3 W3
+  issue_pair(400u, ata[1], 192u, smem_addr(s.w3t), CL_H / 16, ha, TC_KX, CL_H);
+  store_dw(400u, CL_H, CL_H, OFF_W3, OFF_B3, CL_H);
+  make_dz(192u, colZ[1], s.bias + CL_H, true);
+  publish();
+  // ---- layer 2: dW2 (+ db2), dA1 = dZ2 W2
+  issue_pair(256u, ata[0], 336u, smem_addr(s.w2t), CL_H / 16, ha, TC_KX, CL_H);
+  store_dw(256u, CL_H, CL_H, OFF_W2, OFF_B2, CL_H);
+  make_dz(336u, colZ[0], s.bias, false);
+  publish();
+  // ---- layer 1: dW1 (+ db1 from the ones row 67 of xt)
+  issue_pair(400u, xta, 0u, 0u, 0, 0u, 0u, CL_H);
+  store_dw(400u, CL_H, CL_K0, OFF_W1, OFF_B1, CL_IN);
+  tc_free(tmem, TT_COLS);
+}
+
+__global__ void grad_reduce_kernel(const float* __restrict__ gw, int nparts, float* __restrict__ grad,
                                    const float* __restrict__ lossw, float* __restrict__ loss) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p < CL_NPARAM) {
     float s = 0.f;
-    for (int w = 0; w < nwarps; ++w) s += gw[(size_t)w * CL_NPARAM + p];
+    for (int w = 0; w < nparts; ++w) s += gw[(size_t)w * CL_NPARAM + p];
     grad[p] = s;
   }
   if (p == 0) {
     float s = 0.f;
-    for (int w = 0; w < nwarps; ++w) s += lossw[w];
+    for (int w = 0; w < nparts; ++w) s += lossw[w];
     *loss = s;
   }
 }
@@ -756,12 +743,9 @@ __global__ void image_kernel(const float* __restrict__ p, bf16* __restrict__ img
     } else if (e < IMG_W3T) {
       const int r = (e - IMG_W2T) / S64, c = (e - IMG_W2T) % S64;  // W2T[i][j] = W2[j][i]
       v = c < CL_H ? p[OFF_W2 + c * CL_H + r] : 0.f;
-    } else if (e < IMG_W4T) {
+    } else {
       const int r = (e - IMG_W3T) / S64, c = (e - IMG_W3T) % S64;
       v = c < CL_H ? p[OFF_W3 + c * CL_H + r] : 0.f;
-    } else {
-      const int r = (e - IMG_W4T) / S16, c = (e - IMG_W4T) % S16;  // W4T[j][o] = W4[o][j]
-      v = c < CL_NO ? p[OFF_W4 + c * CL_H + r] : 0.f;
     }
     img[e] = __float2bfloat16_rn(v);
   }
@@ -827,7 +811,8 @@ __global__ void __launch_bounds__(TC_THREADS) mlp_eval_kernel(const float* __res
 }
 
 constexpr size_t kInferSmem = sizeof(TcSmem);
-constexpr size_t kTrainSmem = sizeof(SmemMLP) + CL_WARPS * sizeof(TrainSmemWarp);
+constexpr size_t kTrainSmem = sizeof(TcTrainSmem);
+static_assert(kTrainSmem <= 227 * 1024, "training tile exceeds the shared memory of a CTA");
 
 static int configure_closure_kernels() {
   static bool done = false;
@@ -875,11 +860,11 @@ struct pmgb_closure {
   float* adam_m = nullptr;
   float* adam_v = nullptr;
   float* grad = nullptr;
-  float* gw = nullptr;          // per-warp partial gradients
+  float* gw = nullptr;          // per-CTA partial gradients
   float* lossw = nullptr;
   float* loss = nullptr;
   bf16* img = nullptr;
-  int gw_warps = 0;
+  int gw_parts = 0;
   bf16* X = nullptr;            // training inputs
   float* T = nullptr;           // training targets (4 per row)
   int cap = 0, count = 0;
@@ -991,11 +976,11 @@ int pmgb_closure_create(pmgb_pm* pm, const pmgb_p3m_config* full_cfg, float redu
   c->ncells = cd.Mx * cd.My * cd.Mz;
   c->cap = std::max(capacity, 0);
   const size_t n = (size_t)std::max(pm->n, 1);
-  c->gw_warps = 4096 / 16;  // largest batch
+  c->gw_parts = 4096 / TC_ROWS;  // largest batch
   if ((rc = cl_alloc(&c->occ_fx, c->ncells)) || (rc = cl_alloc(&c->occ, c->ncells)) ||
       (rc = cl_alloc(&c->params, CL_NPARAM)) || (rc = cl_alloc(&c->adam_m, CL_NPARAM)) ||
       (rc = cl_alloc(&c->adam_v, CL_NPARAM)) || (rc = cl_alloc(&c->grad, CL_NPARAM)) ||
-      (rc = cl_alloc(&c->gw, (size_t)c->gw_warps * CL_NPARAM)) || (rc = cl_alloc(&c->lossw, c->gw_warps)) ||
+      (rc = cl_alloc(&c->gw, (size_t)c->gw_parts * CL_NPARAM)) || (rc = cl_alloc(&c->lossw, c->gw_parts)) ||
       (rc = cl_alloc(&c->loss, 1)) || (rc = cl_alloc(&c->img, IMG_SIZE)) ||
       (rc = cl_alloc(&c->X, (size_t)std::max(c->cap, 1) * CL_K0)) ||
       (rc = cl_alloc(&c->T, (size_t)std::max(c->cap, 1) * 4)) || (rc = cl_alloc(&c->accF, 3 * n)) ||
@@ -1085,6 +1070,9 @@ int pmgb_closure_train(pmgb_closure* c, int epochs, int batch, float lr, float* 
   if (batch < 16 || batch > 4096 || batch % 64) return set_error("batch must be a multiple of 64 in [64, 4096]"), PMGB_EINVAL;
   if (c->count < batch) return set_error("not enough training rows"), PMGB_EINVAL;
   cudaStream_t st = c->pm->st;
+  int rc = configure_closure_kernels();
+  if (rc) return rc;
+  PMGB_CUDA_TRY(cudaMemsetAsync(c->pm->flags + kFlagTimeout, 0, sizeof(int), st));
   int* perm = nullptr;
   PMGB_CUDA_TRY(cudaMalloc(&perm, (size_t)c->count * sizeof(int)));
   std::vector<int> hp(c->count);
@@ -1101,10 +1089,11 @@ int pmgb_closure_train(pmgb_closure* c, int epochs, int batch, float lr, float* 
       return set_error("permutation upload failed"), PMGB_ECUDA;
     }
     for (int b = 0; b < steps_per_epoch; ++b, ++step) {
-      const int nw = batch / 16;
-      closure_train_kernel<<<nw / CL_WARPS, CL_THREADS, kTrainSmem, st>>>(
-          c->X, c->T, perm, b * batch, batch, 1.0f / batch, c->img, c->params, c->gw, c->lossw);
-      grad_reduce_kernel<<<(CL_NPARAM + 255) / 256, 256, 0, st>>>(c->gw, nw, c->grad, c->lossw, c->loss);
+      const int parts = (batch + TC_ROWS - 1) / TC_ROWS;
+      closure_train_kernel<<<parts, TC_THREADS, kTrainSmem, st>>>(c->X, c->T, perm, b * batch, batch,
+                                                                  1.0f / batch, c->img, c->params, c->gw,
+                                                                  c->lossw, c->pm->flags + kFlagTimeout);
+      grad_reduce_kernel<<<(CL_NPARAM + 255) / 256, 256, 0, st>>>(c->gw, parts, c->grad, c->lossw, c->loss);
       ++c->adam_t;
       // cosine decay to 5% of lr
       const float frac = total_steps > 1 ? (float)step / (float)(total_steps - 1) : 1.f;
@@ -1123,9 +1112,12 @@ int pmgb_closure_train(pmgb_closure* c, int epochs, int batch, float lr, float* 
       }
     }
   }
+  int timed_out = 0;
+  cudaMemcpyAsync(&timed_out, c->pm->flags + kFlagTimeout, sizeof(int), cudaMemcpyDeviceToHost, st);
   cudaError_t err = cudaStreamSynchronize(st);
   cudaFree(perm);
   if (err != cudaSuccess) return set_error(std::string("training: ") + cudaGetErrorString(err)), PMGB_ECUDA;
+  if (timed_out) return set_error("training: a bounded device wait gave up"), PMGB_ETIMEOUT;
   if (final_loss) *final_loss = last;
   return PMGB_OK;
 }
@@ -1345,17 +1337,20 @@ int pmgb_mlp_gradients(const float* params, int n, const float* x, const float* 
   if (rc) return rc;
   float *dp = nullptr, *dt = nullptr, *gw = nullptr, *g = nullptr, *lw = nullptr, *l = nullptr;
   bf16 *img = nullptr, *dx = nullptr;
-  int* perm = nullptr;
-  const int nw = n / 16;
-  PMGB_CUDA_TRY(cudaMalloc(&dp, CL_NPARAM * sizeof(float)));
-  PMGB_CUDA_TRY(cudaMalloc(&img, IMG_SIZE * sizeof(bf16)));
-  PMGB_CUDA_TRY(cudaMalloc(&dx, (size_t)n * CL_K0 * sizeof(bf16)));
-  PMGB_CUDA_TRY(cudaMalloc(&dt, (size_t)n * 4 * sizeof(float)));
-  PMGB_CUDA_TRY(cudaMalloc(&gw, (size_t)nw * CL_NPARAM * sizeof(float)));
-  PMGB_CUDA_TRY(cudaMalloc(&g, CL_NPARAM * sizeof(float)));
-  PMGB_CUDA_TRY(cudaMalloc(&lw, nw * sizeof(float)));
-  PMGB_CUDA_TRY(cudaMalloc(&l, sizeof(float)));
-  PMGB_CUDA_TRY(cudaMalloc(&perm, n * sizeof(int)));
+  int *perm = nullptr, *derr = nullptr;
+  const int parts = (n + TC_ROWS - 1) / TC_ROWS;
+  auto release = [&]() {
+    void* all[] = {dp, dt, gw, g, lw, l, img, dx, perm, derr};
+    for (void* p : all) cudaFree(p);
+  };
+  if (cudaMalloc(&dp, CL_NPARAM * sizeof(float)) || cudaMalloc(&img, IMG_SIZE * sizeof(bf16)) ||
+      cudaMalloc(&dx, (size_t)n * CL_K0 * sizeof(bf16)) || cudaMalloc(&dt, (size_t)n * 4 * sizeof(float)) ||
+      cudaMalloc(&gw, (size_t)parts * CL_NPARAM * sizeof(float)) || cudaMalloc(&g, CL_NPARAM * sizeof(float)) ||
+      cudaMalloc(&lw, parts * sizeof(float)) || cudaMalloc(&l, sizeof(float)) ||
+      cudaMalloc(&perm, n * sizeof(int)) || cudaMalloc(&derr, sizeof(int))) {
+    release();
+    return set_error("device allocation failed"), PMGB_ECUDA;
+  }
   std::vector<bf16> hx((size_t)n * CL_K0);
   std::vector<float> ht((size_t)n * 4, 0.f);
   std::vector<int> hp(n);
@@ -1368,17 +1363,21 @@ int pmgb_mlp_gradients(const float* params, int n, const float* x, const float* 
   cudaMemcpy(dx, hx.data(), hx.size() * sizeof(bf16), cudaMemcpyHostToDevice);
   cudaMemcpy(dt, ht.data(), ht.size() * sizeof(float), cudaMemcpyHostToDevice);
   cudaMemcpy(perm, hp.data(), hp.size() * sizeof(int), cudaMemcpyHostToDevice);
+  cudaMemset(derr, 0, sizeof(int));
   image_kernel<<<64, 256>>>(dp, img);
-  closure_train_kernel<<<nw / CL_WARPS, CL_THREADS, kTrainSmem>>>(dx, dt, perm, 0, n, 1.0f / n, img, dp, gw, lw);
-  grad_reduce_kernel<<<(CL_NPARAM + 255) / 256, 256>>>(gw, nw, g, lw, l);
+  closure_train_kernel<<<parts, TC_THREADS, kTrainSmem>>>(dx, dt, perm, 0, n, 1.0f / n, img, dp, gw, lw, derr);
+  grad_reduce_kernel<<<(CL_NPARAM + 255) / 256, 256>>>(gw, parts, g, lw, l);
+  count_launches(3);
   cudaMemcpy(grad, g, CL_NPARAM * sizeof(float), cudaMemcpyDeviceToHost);
   float lh = 0.f;
+  int timed_out = 0;
   cudaMemcpy(&lh, l, sizeof(float), cudaMemcpyDeviceToHost);
+  cudaMemcpy(&timed_out, derr, sizeof(int), cudaMemcpyDeviceToHost);
   cudaError_t err = cudaDeviceSynchronize();
   if (loss) *loss = lh / n;
-  void* ptrs[] = {dp, dt, gw, g, lw, l, img, dx, perm};
-  for (void* p : ptrs) cudaFree(p);
+  release();
   if (err != cudaSuccess) return set_error(cudaGetErrorString(err)), PMGB_ECUDA;
+  if (timed_out) return set_error("a bounded device wait gave up"), PMGB_ETIMEOUT;
   return PMGB_OK;
 }
 
