@@ -293,6 +293,15 @@ int pmgb_p3m_pair_count(pmgb_p3m* p3m, unsigned long long* ordered_pairs);
 /* Turns the in-range pair counter of force evaluations on or off (off by default; counting
  * costs a few percent of the pair pass). */
 int pmgb_p3m_set_pair_counting(pmgb_p3m* p3m, int enable);
+/* Each pair once, as the reference's half-shell pass (source/p3mMethod.cpp:247-273, 296-322)
+ * does: with y-sorted lists and equal masses the pair pass evaluates the sub-column pairs that
+ * one warp can take whole once, writing both particles' partial forces to slots of their own,
+ * and the rest from both sides.  On by default where it applies; off evaluates every pair from
+ * both sides.  Both are deterministic; they differ by float rounding.  units_last_pass
+ * (may be NULL): the sub-column pairs the last force evaluation took once (0 when it ran
+ * one-sided).  No reference counterpart (a switch of this implementation). */
+int pmgb_p3m_set_symmetric(pmgb_p3m* p3m, int enable);
+int pmgb_p3m_get_symmetric(pmgb_p3m* p3m, int* enabled, unsigned int* units_last_pass);
 
 /* ---------------------------------------------------------------- ensemble ----------- */
 /* No counterpart in the reference (one system per process there).  n_systems independent PM

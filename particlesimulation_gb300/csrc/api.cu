@@ -202,7 +202,7 @@ int force(pmgb_pm* h, int kdk, float kick, int drift, int tag, bool timed) {
                    kick, drift, kdk, h->pm[1 - h->cur], h->vi[1 - h->cur], h->acc,
                    q->count_pairs ? q->npairs : nullptr, stop,
                    h->num_sms, timed ? h->ev[4] : nullptr, h->st, h->equal_mass, q->slots, n,
-                   q->unit_stride);
+                   q->unit_stride, &q->sym);
   if (rc) return rc;
   if (kdk) {
     h->cur = 1 - h->cur;
@@ -721,6 +721,33 @@ int p3m_create_internal(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out,
     pmgb_p3m_destroy(q);
     return rc;
   }
+  // the symmetric part of the pair pass (y-sorted 3 x 3 sub-columns): 243 slots per particle,
+  // 8 mask words per sub-column, the unit list; left off if the memory is not there
+  if (q->cd.sub == 3 && pm->n > 0) {
+    const size_t n = (size_t)pm->n;
+    q->sym.cap = (u32)sym_unit_capacity(q->nsub, pm->n);
+    void* ptr[4] = {nullptr, nullptr, nullptr, nullptr};
+    const size_t bytes[4] = {243 * n * sizeof(float4), ((size_t)q->nsub + 1) * 8 * sizeof(u32),
+                             3 * (size_t)q->sym.cap * sizeof(uint2), n * sizeof(int)};
+    bool ok = true;
+    for (int i = 0; i < 4 && ok; ++i)
+      if (cudaMalloc(&ptr[i], bytes[i]) != cudaSuccess) {
+        ptr[i] = nullptr;
+        ok = false;
+      }
+    if (ok) {
+      q->sym.slots = (float4*)ptr[0];
+      q->sym.masks = (u32*)ptr[1];
+      q->sym.units = (uint2*)ptr[2];
+      q->sym.subcol = (int*)ptr[3];
+      q->sym.enabled = 1;
+    } else {
+      for (void* p : ptr)
+        if (p) cudaFree(p);
+      cudaGetLastError();
+      q->sym = SymPass{};
+    }
+  }
   if (cudaMemcpyAsync(q->table, q->table_h, 1000 * sizeof(float), cudaMemcpyHostToDevice, pm->st) != cudaSuccess ||
       cudaMemsetAsync(q->npairs, 0, sizeof(unsigned long long), pm->st) != cudaSuccess ||
       cudaStreamSynchronize(pm->st) != cudaSuccess) {
@@ -743,7 +770,7 @@ int pmgb_p3m_destroy(pmgb_p3m* q) {
     q->pm->since_sort = 1 << 30;
   }
   void* ptrs[] = {q->cell_start, q->item_cnt, q->item_off, q->scan_tmp, q->nitems, q->counter, q->items, q->table,
-                  q->npairs, q->slots, q->heavy};
+                  q->npairs, q->slots, q->heavy, q->sym.slots, q->sym.masks, q->sym.units, q->sym.subcol};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete q;
@@ -808,6 +835,24 @@ int pmgb_p3m_get_cell_lists(pmgb_p3m* q, int* order, int* counts, int* dims3) {
 int pmgb_p3m_set_pair_counting(pmgb_p3m* q, int enable) {
   if (!q) return set_error("null handle"), PMGB_EINVAL;
   q->count_pairs = enable ? 1 : 0;
+  return PMGB_OK;
+}
+
+int pmgb_p3m_set_symmetric(pmgb_p3m* q, int enable) {
+  if (!q) return set_error("null handle"), PMGB_EINVAL;
+  q->sym.enabled = enable && q->sym.slots ? 1 : 0;
+  return PMGB_OK;
+}
+
+int pmgb_p3m_get_symmetric(pmgb_p3m* q, int* enabled, unsigned int* units_last_pass) {
+  if (!q || !enabled) return set_error("null argument"), PMGB_EINVAL;
+  *enabled = q->sym.enabled;
+  if (units_last_pass) {
+    // counter word 28 of the slotted pass: the symmetric units it listed
+    PMGB_CUDA_TRY(cudaMemcpyAsync(units_last_pass, q->counter + 28, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                                  q->pm->st));
+    PMGB_CUDA_TRY(cudaStreamSynchronize(q->pm->st));
+  }
   return PMGB_OK;
 }
 

@@ -47,12 +47,26 @@ int launch_unpack(const float4* pm, const float4* vi, const float4* acc, int n, 
                   int orig, float* pos, float* vel, float* aout, cudaStream_t st);
 int launch_pack(const float* pos, const float* vel, const float* mass_code, int n, float H,
                 float DT, int orig, float4* pm, float4* vi, cudaStream_t st);
+// Buffers of the pair pass's symmetric part (pair.cu): dense sub-column pairs below a cost
+// bound are evaluated once per pair, each side's partial force going to a slot of its own
+// (direction, neighbour sub-column); the rest stays one-sided.
+struct SymPass {
+  float4* slots = nullptr;  // 243 x n partial accelerations, slot = direction * 9 + sub-column
+  u32* masks = nullptr;     // 8 words per sub-column (nsub + 1): which slots the pass used
+  uint2* units = nullptr;   // 3 cap: staged units (cap x 16 B), then the list (i side, j side)
+  u32 cap = 0;              // units a pass can list
+  int* subcol = nullptr;    // sub-column of each particle (sorted order)
+  int enabled = 0;          // the handle's switch (pmgb_p3m_set_symmetric)
+};
+int sym_unit_capacity(int nsub, int n);
+
 int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const int* cell_start,
                 const ChainDims& cd, u32* item_cnt, u32* item_off, u32* scan_tmp, u32* nitems, int2* items,
                 int nitems_max, u32* heavy, u32* counter, const PairParams& pp, const float* table,
                 const StepParams& sp, float kick, int drift, int kdk, float4* pm_out, float4* vi_out,
                 float4* acc_out, unsigned long long* npairs, int* stop, int num_sms, cudaEvent_t ev_pair,
-                cudaStream_t st, int equal_mass, float4* slots, int n, int unit_stride = 1);
+                cudaStream_t st, int equal_mass, float4* slots, int n, int unit_stride = 1,
+                const SymPass* sym = nullptr);
 // Sampled pair passes (unit_stride > 1, slotted passes only: pair_pass_sampleable): flags[id] = 1
 // for the particles of the slices such a pass covered (original index order).
 bool pair_pass_sampleable(const PairParams& pp);
@@ -131,6 +145,7 @@ struct pmgb_p3m {
   int count_pairs = 0;  // count in-range pairs during force evaluations (pmgb_p3m_set_pair_counting)
   float4* slots = nullptr;  // 27 x n partial short-range accelerations (pair.cu, table pass)
   int unit_stride = 1;      // > 1: the next passes cover every unit_stride-th slice only (judge)
+  pmgb::SymPass sym{};      // symmetric sub-column pairs (y-sorted lists only)
 };
 
 namespace pmgb {

@@ -9,10 +9,12 @@
 //
 // GPU formulation.  The reference walks 13 half-shell neighbour cells and scatters -F_ij into
 // per-neighbour slots of j.  Here each particle gathers from all 27 cells (each pair is
-// evaluated twice, once per side), so no scatter, no atomics and a deterministic result.
-// Two kernels: pair_slot_kernel (below; the table pass of every run, finer work items and
-// fewer instructions per pair) and pair_kernel, described here, which also counts pairs and
-// evaluates the table-free formula.
+// evaluated twice, once per side), so no scatter, no atomics and a deterministic result, except
+// for the dense sub-column pairs of equal-mass systems, which the slotted pass evaluates once,
+// both sides into slots of their own (the symmetric part, below).
+// Two kernels: pair_slot_kernel (below; the table pass and the exact formula of every run,
+// finer work items and fewer instructions per pair) and pair_kernel, described here, which also
+// counts pairs and evaluates the softened table-free formula.
 // Work items are 32-particle slices of one cell (the cells are y-sorted, so a slice spans a
 // narrow y range); a warp takes items from a global counter (dense cells cost more, the counter
 // balances).  For each neighbour cell a lane binary-searches the y window
@@ -24,7 +26,9 @@
 // The epilogue adds the PM acceleration and, in a run, applies the kick, the drift, the unit
 // round trip and the escape test, writing the new state to separate buffers (other warps still
 // read the old positions).
-#include "common.cuh"
+#include <algorithm>
+
+#include "handles.cuh"
 
 namespace pmgb {
 
@@ -249,10 +253,21 @@ constexpr int SLOT_THREADS = 512;
 constexpr int SLOT_WARPS = SLOT_THREADS / 32;
 constexpr int SLOT_CTAS_PER_SM = 1;         // resident CTAs per SM (128 registers per thread)
 // staging (SLOT_WARPS x 32 float4) + CTA partial sums (SLOT_WARPS x SLOT_SLICE float4) + table
-constexpr int SLOT_SMEM = SLOT_WARPS * 32 * 16 + SLOT_WARPS * SLOT_SLICE * 16 + SLOT_TAB * SLOT_REP * 8;
+constexpr int SLOT_PART = 128;              // partial sums per warp (the symmetric slices' 128)
+constexpr int SLOT_SMEM = SLOT_WARPS * 32 * 16 + SLOT_WARPS * SLOT_PART * 16 + SLOT_TAB * SLOT_REP * 8;
 // Units whose estimated cost reaches 1/SLOT_HEAVY_DIV of a warp's share of the pass (and at
 // least SLOT_HEAVY_MIN) are taken by whole CTAs.
 constexpr int SLOT_HEAVY_DIV = 4;
+// symmetric sub-column pairs: 3 x 3 sub-columns per cell, one slot per (direction, neighbour
+// sub-column) and particle, 243 bits of which per sub-column
+constexpr int SYM_LOCAL = 9;
+constexpr int SYM_NSLOT = NNB * SYM_LOCAL;
+constexpr int SYM_MASK_WORDS = (SYM_NSLOT + 31) / 32;
+// counter words of the slotted pass (see SLOT_COUNTER_WORDS)
+// symmetric units in cost buckets (longest first): 0..3 for CTAs (|p| |q| >= 8, 2, 1/2, 1/4
+// heavy thresholds), 4..8 for warps (>= 1/8, 1/16, 1/32, 1/64 of the threshold, below)
+constexpr int SYM_NB = 9, SYM_NB_CTA = 4;
+constexpr int SLOT_SYM_COUNT = 10, SLOT_SYM_TAKEN = SLOT_SYM_COUNT + SYM_NB, SLOT_SYM_TOTAL = SLOT_SYM_TAKEN + SYM_NB;
 constexpr unsigned long long SLOT_HEAVY_MIN = 64ull * 1024;
 
 struct SlotI {
@@ -359,6 +374,9 @@ struct SlotCtx {
   float re2, sc, gap_margin;
   int ysort;
   float cn;  // EXACT: Newton coefficient -G m / re^2 in the scaled coordinates
+  // symmetric part of the pass (null when off): bit k * 9 + q of sub-column a's 8 words marks
+  // neighbour sub-column q of direction k as evaluated by the symmetric units instead
+  const u32* __restrict__ sym_masks;
 };
 
 // One work unit: the slice items[it / 27] against neighbour cell it % 27, into slot k of the
@@ -411,6 +429,10 @@ __device__ __forceinline__ void slot_unit(const SlotCtx& c, u32 it, float4 (*jbu
       const float gzs = fmaxf(fmaxf(jz0 - (iz0 + cd.HCsz), iz0 - (jz0 + cd.HCsz)) - c.gap_margin, 0.f);
       const float g2 = gxs * gxs + gzs * gzs;
       if (g2 >= c.re2) continue;
+      if (c.sym_masks) {
+        const int sb = k * SYM_LOCAL + qs;
+        if ((__ldg(&c.sym_masks[(size_t)item.x * SYM_MASK_WORDS + (sb >> 5)]) >> (sb & 31)) & 1u) continue;
+      }
       // a pair in range has |dy|^2 < re^2 - (its x-z distance)^2 <= re^2 - g2: the y window
       // of this sub-column is the chord of the cutoff sphere at the sub-column's x-z gap, widened
       // by 1e-5 of the coordinates' size against float rounding of the comparisons
@@ -493,18 +515,339 @@ __device__ __forceinline__ void slot_unit(const SlotCtx& c, u32 it, float4 (*jbu
 // others idle; then every warp takes the medium units (cost in [thr / 4, thr), listed from the
 // far end of the same buffer, counter[1]), then the rest in unit order (counter[8]).  If the
 // lists overflowed the buffer, every unit is taken by the last loop.
-template <bool EQM, bool EXACT>
-__global__ void __maxnreg__(128) pair_slot_kernel(
-    const float4* __restrict__ pm, int n, const int* __restrict__ cell_start,
-    const int2* __restrict__ items, const u32* __restrict__ nitems_p, const u32* __restrict__ heavy,
-    u32 heavy_cap, u32* __restrict__ counter, ChainDimsP cd, PairParams pp, const float* __restrict__ table,
-    float4* __restrict__ slots, u32 unit_stride, const int* __restrict__ stop) {
+// ------------------------------------------------ symmetric sub-column pairs ------------
+// The reference evaluates each pair once (half shell of 13 neighbour cells, the j side written
+// to per-neighbour slots of j: source/p3mMethod.cpp:247-273, 296-322).  Here the same holds for
+// the dense sub-column pairs (p, q): both lists non-empty, the larger at least SYM_MIN_BIG
+// particles and the smaller SYM_MIN_SMALL, x-z gap below the cutoff, |p| |q| below
+// SYM_CTA_MUL heavy thresholds of the one-sided pass (denser pairs stay one-sided, where whole
+// CTAs share their units).  One unit per such pair (listed from its upper-half side: direction
+// k > 13, or k = 13 and the higher local index); its i side p is the larger list, its j side q.
+// The unit runs p's 128-particle slices (4 per lane) against their y windows in q and writes
+//   * the i side into slot (k, local index of q) of p's particles (one store per slice), and
+//   * the j side into slot (26 - k, local index of p) of q's particles: the lanes' products for
+//     4 candidates are summed across the warp by a transposing butterfly of 18 shuffles (no
+//     selects: the lanes visit the 4 candidates of a group in an order swizzled by lane bits 4
+//     and 3, so that every lane sends and keeps the same registers), each lane keeping one
+//     candidate's total per chunk of 32, added to the slot (cleared at the unit's start;
+//     read-modify-written by one warp at a time, in slice order).
+// Units of cost |p| |q| >= 1/4 of the heavy threshold are taken by whole CTAs (the warps split each
+// window's chunks, the i sides added in warp order through shared memory), the rest by warps.
+// Every slot has one writer at a time and a fixed summation order: the result is deterministic.
+// The one-sided pass skips the pairs marked in the sub-column's mask and the epilogue adds the
+// marked slots after each direction's one-sided slot.  Equal masses only (the mass is folded in
+// the table); sampled passes stay one-sided.
+constexpr int SYM_IPL = 4;                // i particles per lane
+constexpr int SYM_SLICE = 32 * SYM_IPL;   // particles per slice of a unit's i side
+constexpr int SYM_MIN_BIG = 128;          // the larger list of a symmetric pair, at least
+constexpr int SYM_MIN_SMALL = 16;         // the smaller one, at least
+constexpr unsigned long long SYM_CTA_MUL = 16;  // |p| |q| below 16 heavy thresholds
+
+struct SymI {
+  float x, y, z;
+  float sx, sy, sz, cx, cy, cz;
+  float px, py, pz;
+};
+
+// Squared x-z gap between sub-columns (cell x gx, z gz, local ca) and (nx, nz, cb), computed the
+// same way in either order (min / max, no contraction), so that the marks are symmetric.
+__device__ __forceinline__ float sym_gap2(const ChainDimsP& cd, int gx, int gz, int ca, int nx, int nz, int cb,
+                                          float margin) {
+  const float ax = (float)(gx * cd.sub + ca % cd.sub) * cd.HCsx, az = (float)(gz * cd.sub + ca / cd.sub) * cd.HCsz;
+  const float bx = (float)(nx * cd.sub + cb % cd.sub) * cd.HCsx, bz = (float)(nz * cd.sub + cb / cd.sub) * cd.HCsz;
+  const float gxs = fmaxf(__fsub_rn(__fsub_rn(fmaxf(ax, bx), __fadd_rn(fminf(ax, bx), cd.HCsx)), margin), 0.f);
+  const float gzs = fmaxf(__fsub_rn(__fsub_rn(fmaxf(az, bz), __fadd_rn(fminf(az, bz), cd.HCsz)), margin), 0.f);
+  return __fadd_rn(__fmul_rn(gxs, gxs), __fmul_rn(gzs, gzs));
+}
+
+// Marks and units, one thread per sub-column a (a = nsub: the bucket outside the mesh, no marks).
+// Each unit is staged as (p, q, bucket, position in its bucket); sym_scatter_kernel then lays
+// the buckets out one after the other in units.  If more than cap units are listed, the pass
+// runs one-sided.
+__device__ __forceinline__ int sym_bucket(unsigned long long c, unsigned long long thr) {
+  if (4 * c >= thr) return c >= 8 * thr ? 0 : c >= 2 * thr ? 1 : 2 * c >= thr ? 2 : 3;
+  return 8 * c >= thr ? 4 : 16 * c >= thr ? 5 : 32 * c >= thr ? 6 : 64 * c >= thr ? 7 : 8;
+}
+
+__global__ void sym_plan_kernel(const int* __restrict__ cs, ChainDimsP cd, int nsub, float re2, float margin,
+                                u32* __restrict__ masks, uint4* __restrict__ stage, u32 cap,
+                                u32* __restrict__ counter, const int* __restrict__ stop) {
   if (*stop) return;
-  extern __shared__ float4 slot_smem[];
-  __shared__ u32 s_unit;
-  float4 (*jbuf)[32] = reinterpret_cast<float4 (*)[32]>(slot_smem);
-  float4* part = slot_smem + SLOT_WARPS * 32;
-  float2* tab_all = reinterpret_cast<float2*>(part + SLOT_WARPS * SLOT_SLICE);
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a > nsub) return;
+  u32 w[SYM_MASK_WORDS];
+#pragma unroll
+  for (int i = 0; i < SYM_MASK_WORDS; ++i) w[i] = 0u;
+  const int pa = a < nsub ? cs[a + 1] - cs[a] : 0;
+  if (pa >= SYM_MIN_SMALL) {
+    const unsigned long long thr = __ldcg(reinterpret_cast<const unsigned long long*>(counter + 6));
+    const int cell = a / SYM_LOCAL, ca = a % SYM_LOCAL;
+    const int gx = cell % cd.Mx, gy = (cell / cd.Mx) % cd.My, gz = cell / (cd.Mx * cd.My);
+    for (int k = 0; k < NNB; ++k) {
+      const int nx = gx + k % 3 - 1, ny = gy + (k / 3) % 3 - 1, nz = gz + k / 9 - 1;
+      if (nx < 0 || ny < 0 || nz < 0 || nx >= cd.Mx || ny >= cd.My || nz >= cd.Mz) continue;
+      const int nb = nx + ny * cd.Mx + nz * cd.Mx * cd.My;
+#pragma unroll
+      for (int cb = 0; cb < SYM_LOCAL; ++cb) {
+        const int b = nb * SYM_LOCAL + cb;
+        if (b == a) continue;
+        const int pb = __ldg(&cs[b + 1]) - __ldg(&cs[b]);
+        if (pb < SYM_MIN_SMALL || max(pa, pb) < SYM_MIN_BIG) continue;
+        const unsigned long long cost = (unsigned long long)pa * (unsigned long long)pb;
+        if (cost >= thr * SYM_CTA_MUL) continue;
+        if (sym_gap2(cd, gx, gz, ca, nx, nz, cb, margin) >= re2) continue;
+        const int sb = k * SYM_LOCAL + cb;
+#pragma unroll
+        for (int i = 0; i < SYM_MASK_WORDS; ++i)
+          if ((sb >> 5) == i) w[i] |= 1u << (sb & 31);
+        if (k > 13 || (k == 13 && cb > ca)) {
+          const int bk = sym_bucket(cost, thr);
+          const u32 pos = atomicAdd(&counter[SLOT_SYM_COUNT + bk], 1u);
+          const u32 idx = atomicAdd(&counter[SLOT_SYM_TOTAL], 1u);
+          if (idx < cap)
+            stage[idx] = pa >= pb ? make_uint4((u32)a, (u32)b, (u32)bk, pos) : make_uint4((u32)b, (u32)a, (u32)bk, pos);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < SYM_MASK_WORDS; ++i) masks[(size_t)a * SYM_MASK_WORDS + i] = w[i];
+}
+
+// subcol[i] = the sub-column (or the outside bucket) of sorted particle i.
+__global__ void subcol_kernel(const int* __restrict__ cs, const int2* __restrict__ items,
+                              const u32* __restrict__ nitems_p, int* __restrict__ subcol,
+                              const int* __restrict__ stop) {
+  if (*stop) return;
+  const u32 it = blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= *nitems_p) return;
+  const int2 item = items[it];
+  const int end = min(item.y + SLOT_SLICE, cs[item.x + 1]);
+  for (int i = item.y; i < end; ++i) subcol[i] = item.x;
+}
+
+// Start of each bucket in the laid-out unit list (exclusive prefix of the bucket counts).
+__device__ __forceinline__ u32 sym_bucket_start(const u32* __restrict__ counter, int b) {
+  u32 off = 0;
+#pragma unroll
+  for (int i = 0; i < SYM_NB; ++i)
+    if (i < b) off += __ldcg(&counter[SLOT_SYM_COUNT + i]);
+  return off;
+}
+
+// Lays the staged units out bucket after bucket (positions within a bucket as staged).
+__global__ void sym_scatter_kernel(const uint4* __restrict__ stage, uint2* __restrict__ units, u32 cap,
+                                   const u32* __restrict__ counter, const int* __restrict__ stop) {
+  if (*stop) return;
+  const u32 total = __ldcg(&counter[SLOT_SYM_TOTAL]);
+  if (total > cap) return;
+  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const uint4 e = stage[i];
+    units[sym_bucket_start(counter, (int)e.z) + e.w] = make_uint2(e.x, e.y);
+  }
+}
+
+// One candidate q against the lane's SYM_IPL i particles: their sums accumulate as in slot_pair;
+// v = the sum of the pair forces f d, the candidate's share of its j side (negated later).
+// MASKED: each force is multiplied by w[u] (0 for lanes past a slice's end, which hold copies
+// of its last particle, and for candidates past a chunk's end: neither may reach a sum).
+template <bool EXACT, bool MASKED>
+__device__ __forceinline__ void sym_pair(SymI (&I)[SYM_IPL], const float4& q, u32 tab_base, float cn,
+                                         const float (&w)[SYM_IPL], float (&v)[3]) {
+#pragma unroll
+  for (int u = 0; u < SYM_IPL; ++u) {
+    const float dx = I[u].x - q.x, dy = I[u].y - q.y, dz = I[u].z - q.z;
+    float xs;
+    asm("fma.rn.sat.f32 %0, %1, %1, %2;" : "=f"(xs)
+        : "f"(dz), "f"(fmaf(dy, dy, EXACT ? fmaf(dx, dx, 1e-20f) : dx * dx)));
+    const u32 bits = __float_as_uint(__fmaf_rd(xs, EXACT ? 499.0f : 512.0f, kMagic));
+    float2 ab;
+    asm("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(ab.x), "=f"(ab.y) : "r"(bits * (SLOT_REP * 8) + tab_base));
+    float f = fmaf(xs, ab.y, ab.x);
+    if (EXACT) {
+      const float ri = rsqrt_approx(xs);
+      f = fmaf(cn, ri * ri * ri, f);
+    }
+    if (MASKED) f *= w[u];
+    I[u].px = fmaf(f, dx, I[u].px);
+    I[u].py = fmaf(f, dy, I[u].py);
+    I[u].pz = fmaf(f, dz, I[u].pz);
+    if (u == 0) {
+      v[0] = f * dx;
+      v[1] = f * dy;
+      v[2] = f * dz;
+    } else {
+      v[0] = fmaf(f, dx, v[0]);
+      v[1] = fmaf(f, dy, v[1]);
+      v[2] = fmaf(f, dz, v[2]);
+    }
+  }
+}
+
+// The candidates [jb, je) of q against the slice in I (scaled coordinates, origin (ox, ys0, oz)):
+// i sides into I's sums, j sides read-modified-written in sj.  COOP: this warp takes the chunks
+// warp, warp + SLOT_WARPS, ... of the window.
+template <bool EXACT, bool MASKED, bool COOP>
+__device__ __forceinline__ void sym_window(const SlotCtx& c, SymI (&I)[SYM_IPL], const float (&w)[SYM_IPL],
+                                           int jb, int je, float ox, float ys0, float oz, float4* __restrict__ sj,
+                                           float4 (*jbuf)[32], u32 tab_base, int lane, int warp) {
+  const int swz = (lane >> 3) & 3;     // candidate order within a group of 4: m ^ swz
+  const int own = 4 * (lane & 7) + swz;  // this lane's candidate total of each chunk
+  const float sc = c.sc;
+  const int jstep = COOP ? 32 * SLOT_WARPS : 32;
+  for (int j0 = jb + (COOP ? 32 * warp : 0); j0 < je; j0 += jstep) {
+    const int jj = j0 + lane;
+    float4 qj = jj < je ? c.pm[jj] : make_float4(3.0e30f, 3.0e30f, 3.0e30f, 0.f);
+    qj.x = (qj.x - ox) * sc;
+    qj.y = (qj.y - ys0) * sc;
+    qj.z = (qj.z - oz) * sc;
+    jbuf[warp][lane] = qj;
+    const int jo = j0 + own;
+    const float4 old = jo < je ? sj[jo] : make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncwarp();
+    const int cnt = min(32, je - j0);
+#pragma unroll
+    for (int u = 0; u < SYM_IPL; ++u) I[u].px = I[u].py = I[u].pz = 0.f;
+    float tx = 0.f, ty = 0.f, tz = 0.f;
+#pragma unroll 1
+    for (int g = 0; 4 * g < cnt; ++g) {
+      float v[4][3];
+      if (4 * g + 4 <= cnt) {
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+          sym_pair<EXACT, MASKED>(I, jbuf[warp][4 * g + (m ^ swz)], tab_base, c.cn, w, v[m]);
+      } else {
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          const float cw = 4 * g + (m ^ swz) < cnt ? 1.f : 0.f;
+          float wm[SYM_IPL];
+#pragma unroll
+          for (int u = 0; u < SYM_IPL; ++u) wm[u] = MASKED ? w[u] * cw : cw;
+          sym_pair<EXACT, true>(I, jbuf[warp][4 * g + (m ^ swz)], tab_base, c.cn, wm, v[m]);
+        }
+      }
+      // lanes l and l ^ 16 hold each other's slots 2, 3 in their slots 0, 1 (swz differs in bit
+      // 1), lanes l and l ^ 8 each other's slot 1 in their slot 0 (bit 0); then bits 2..0
+      float x[3];
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc) {
+        const float w0 = v[0][cc] + __shfl_xor_sync(0xFFFFFFFFu, v[2][cc], 16);
+        const float w1 = v[1][cc] + __shfl_xor_sync(0xFFFFFFFFu, v[3][cc], 16);
+        float t = w0 + __shfl_xor_sync(0xFFFFFFFFu, w1, 8);
+        t += __shfl_xor_sync(0xFFFFFFFFu, t, 4);
+        t += __shfl_xor_sync(0xFFFFFFFFu, t, 2);
+        t += __shfl_xor_sync(0xFFFFFFFFu, t, 1);
+        x[cc] = t;
+      }
+      if ((lane & 7) == g) {
+        tx = x[0];
+        ty = x[1];
+        tz = x[2];
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int u = 0; u < SYM_IPL; ++u) {
+      kahan_add(I[u].sx, I[u].cx, I[u].px);
+      kahan_add(I[u].sy, I[u].cy, I[u].py);
+      kahan_add(I[u].sz, I[u].cz, I[u].pz);
+    }
+    if (jo < je) sj[jo] = make_float4(old.x - tx, old.y - ty, old.z - tz, 0.f);
+    __syncwarp();
+  }
+}
+
+// One symmetric unit (i side p, j side q) by one warp, or by the whole CTA (COOP; part:
+// SLOT_WARPS x SYM_SLICE partial sums).
+template <bool EXACT, bool COOP>
+__device__ __forceinline__ void sym_unit(const SlotCtx& c, float4* __restrict__ sym_slots, uint2 unit,
+                                         float4 (*jbuf)[32], float4* part, u32 tab_base, int lane, int warp) {
+  const ChainDimsP& cd = c.cd;
+  const int p = (int)unit.x, q = (int)unit.y;
+  const int cp = p / SYM_LOCAL, ca = p % SYM_LOCAL, cq = q / SYM_LOCAL, cb = q % SYM_LOCAL;
+  const int gx = cp % cd.Mx, gy = (cp / cd.Mx) % cd.My, gz = cp / (cd.Mx * cd.My);
+  const int nx = cq % cd.Mx, ny = (cq / cd.Mx) % cd.My, nz = cq / (cd.Mx * cd.My);
+  const int k = (nx - gx + 1) + 3 * (ny - gy + 1) + 9 * (nz - gz + 1);
+  float4* __restrict__ si = sym_slots + (size_t)(k * SYM_LOCAL + cb) * c.n;
+  float4* __restrict__ sj = sym_slots + (size_t)((NNB - 1 - k) * SYM_LOCAL + ca) * c.n;
+  const float h0 = sqrtf(c.re2 - sym_gap2(cd, gx, gz, ca, nx, nz, cb, c.gap_margin));
+  const int bb = c.cell_start[q], be = c.cell_start[q + 1];
+  if (COOP) {
+    for (int j = bb + (int)threadIdx.x; j < be; j += SLOT_THREADS) sj[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+  } else {
+    for (int j = bb + lane; j < be; j += 32) sj[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncwarp();
+  }
+  const int cend = c.cell_start[p + 1];
+  const float sc = c.sc;
+  for (int i0 = c.cell_start[p]; i0 < cend; i0 += SYM_SLICE) {
+    const int last = min(i0 + SYM_SLICE - 1, cend - 1);
+    SymI I[SYM_IPL];
+    float w[SYM_IPL];
+#pragma unroll
+    for (int u = 0; u < SYM_IPL; ++u) {
+      const int i = i0 + 32 * u + lane;
+      const float4 pi = c.pm[i < cend ? i : last];
+      I[u].x = pi.x;
+      I[u].y = pi.y;
+      I[u].z = pi.z;
+      I[u].sx = I[u].sy = I[u].sz = I[u].cx = I[u].cy = I[u].cz = 0.f;
+      w[u] = i < cend ? 1.f : 0.f;
+    }
+    const float ys0 = __shfl_sync(0xFFFFFFFFu, I[0].y, 0);
+    const float ys1 = __ldg(&c.pm[last].y);
+    const float ox = __shfl_sync(0xFFFFFFFFu, I[0].x, 0), oz = __shfl_sync(0xFFFFFFFFu, I[0].z, 0);
+#pragma unroll
+    for (int u = 0; u < SYM_IPL; ++u) {
+      I[u].x = (I[u].x - ox) * sc;
+      I[u].y = (I[u].y - ys0) * sc;
+      I[u].z = (I[u].z - oz) * sc;
+    }
+    const float h = h0 + 1e-5f * (1.f + fabsf(ys1));
+    int jb = bb, je = be;
+    if (c.ysort && je > jb) {
+      jb = warp_y_bound<false>(c.pm, jb, je, ys0 - h, lane);
+      je = warp_y_bound<true>(c.pm, jb, je, ys1 + h, lane);
+    }
+    if (i0 + SYM_SLICE <= cend)
+      sym_window<EXACT, false, COOP>(c, I, w, jb, je, ox, ys0, oz, sj, jbuf, tab_base, lane, warp);
+    else
+      sym_window<EXACT, true, COOP>(c, I, w, jb, je, ox, ys0, oz, sj, jbuf, tab_base, lane, warp);
+    if (!COOP) {
+#pragma unroll
+      for (int u = 0; u < SYM_IPL; ++u) {
+        const int i = i0 + 32 * u + lane;
+        if (i < cend) si[i] = make_float4(I[u].sx, I[u].sy, I[u].sz, 0.f);
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < SYM_IPL; ++u)
+        part[warp * SYM_SLICE + 32 * u + lane] = make_float4(I[u].sx, I[u].sy, I[u].sz, 0.f);
+      __syncthreads();
+      if (threadIdx.x < SYM_SLICE) {
+        float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+#pragma unroll 4
+        for (int ww = 0; ww < SLOT_WARPS; ++ww) {
+          const float4 v = part[ww * SYM_SLICE + threadIdx.x];
+          kahan_add(sx, cx, v.x);
+          kahan_add(sy, cy, v.y);
+          kahan_add(sz, cz, v.z);
+        }
+        const int i = i0 + (int)threadIdx.x;
+        if (i < cend) si[i] = make_float4(sx, sy, sz, 0.f);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// The lane-replicated force table of the slotted passes, in shared memory (tab_all, SLOT_TAB x
+// SLOT_REP float2), with the coordinate scale sc and, exact mode, the Newton coefficient cn.
+template <bool EQM, bool EXACT>
+__device__ __forceinline__ void slot_table_setup(const float4* __restrict__ pm, const PairParams& pp,
+                                                 const float* __restrict__ table, float2* tab_all,
+                                                 float& sc_out, float& cn_out) {
   // table: coordinates are scaled by sc = 1/(sqrt(512) delta) (512 sc^2 = 1/delta^2 to float
   // rounding); exact: by sc = 1/re
   const float sc = EXACT ? 1.0f / pp.re : (float)sqrt((double)pp.inv_d2 / 512.0);
@@ -513,7 +856,7 @@ __global__ void __maxnreg__(128) pair_slot_kernel(
   if (!EXACT) {
     // every particle has the same mass when EQM: fold it into the table, with 1/sc
     const double mjs = mj / (double)sc;
-    for (int t = threadIdx.x; t < SLOT_TAB; t += SLOT_THREADS) {
+    for (int t = threadIdx.x; t < SLOT_TAB; t += (int)blockDim.x) {
       float2 ab = make_float2(0.f, 0.f);
       if (t < 499) {
         const float a = table[t];
@@ -532,7 +875,7 @@ __global__ void __maxnreg__(128) pair_slot_kernel(
     const float r1 = rsqrt_approx(1.0f);
     const float c499 = -(cn * (r1 * r1 * r1));
     const double w = mj * re;
-    for (int t = threadIdx.x; t < SLOT_TAB; t += SLOT_THREADS) {
+    for (int t = threadIdx.x; t < SLOT_TAB; t += (int)blockDim.x) {
       float2 ab = make_float2(0.f, 0.f);
       if (t < 499) {
         const double g0 = table[500 + t], g1 = table[500 + t + 1];
@@ -544,6 +887,26 @@ __global__ void __maxnreg__(128) pair_slot_kernel(
       for (int c = 0; c < SLOT_REP; ++c) tab_all[t * SLOT_REP + c] = ab;
     }
   }
+  sc_out = sc;
+  cn_out = cn;
+}
+
+template <bool EQM, bool EXACT>
+__global__ void __maxnreg__(128) pair_slot_kernel(
+    const float4* __restrict__ pm, int n, const int* __restrict__ cell_start,
+    const int2* __restrict__ items, const u32* __restrict__ nitems_p, const u32* __restrict__ heavy,
+    u32 heavy_cap, u32* __restrict__ counter, ChainDimsP cd, PairParams pp, const float* __restrict__ table,
+    float4* __restrict__ slots, u32 unit_stride, const u32* __restrict__ sym_masks, u32 sym_cap,
+    float4* __restrict__ sym_slots, const uint2* __restrict__ sym_units, const int* __restrict__ stop) {
+  static_assert(SLOT_PART >= SLOT_SLICE && SLOT_PART >= SYM_SLICE, "partial-sum buffer too small");
+  if (*stop) return;
+  extern __shared__ float4 slot_smem[];
+  __shared__ u32 s_unit;
+  float4 (*jbuf)[32] = reinterpret_cast<float4 (*)[32]>(slot_smem);
+  float4* part = slot_smem + SLOT_WARPS * 32;
+  float2* tab_all = reinterpret_cast<float2*>(part + SLOT_WARPS * SLOT_PART);
+  float sc, cn;
+  slot_table_setup<EQM, EXACT>(pm, pp, table, tab_all, sc, cn);
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
@@ -551,7 +914,9 @@ __global__ void __maxnreg__(128) pair_slot_kernel(
                        __float_as_uint(kMagic) * (u32)(SLOT_REP * 8);
   // a neighbour sub-column is skipped when its x-z distance from the slice's sub-column is at
   // least the cutoff (with a margin far above the rounding of the sub-column assignment)
-  const SlotCtx c{pm, cell_start, items, slots, n, cd, pp.re2, sc, 1e-3f * fminf(cd.HCsx, cd.HCsz), pp.ysort, cn};
+  const bool sym_on = EQM && sym_masks && __ldcg(&counter[SLOT_SYM_TOTAL]) <= sym_cap;
+  const SlotCtx c{pm, cell_start, items, slots, n, cd, pp.re2, sc, 1e-3f * fminf(cd.HCsx, cd.HCsz), pp.ysort, cn,
+                  sym_on ? sym_masks : nullptr};
   const u32 nall = *nitems_p * NNB;  // every slice once per neighbour cell
   const u32 nh = __ldcg(&counter[2]), nm = __ldcg(&counter[3]);
   const bool listed = (unsigned long long)nh + nm <= heavy_cap;  // both lists complete
@@ -565,6 +930,39 @@ __global__ void __maxnreg__(128) pair_slot_kernel(
     if (h >= nheavy) break;
     slot_unit<EQM, EXACT, true>(c, __ldg(&heavy[h]), jbuf, part, tab_base, lane, warp);
   }
+  if constexpr (EQM) {
+    if (sym_on) {  // the symmetric units of CTAs, longest bucket first
+      for (int b = 0; b < SYM_NB_CTA; ++b) {
+        const u32 cnt = __ldcg(&counter[SLOT_SYM_COUNT + b]), off = sym_bucket_start(counter, b);
+        for (;;) {
+          if (threadIdx.x == 0) s_unit = atomicAdd(&counter[SLOT_SYM_TAKEN + b], 1u);
+          __syncthreads();
+          const u32 h = s_unit;
+          __syncthreads();
+          if (h >= cnt) break;
+          sym_unit<EXACT, true>(c, sym_slots, __ldg(&sym_units[off + h]), jbuf, part, tab_base, lane, warp);
+        }
+      }
+    }
+  }
+  // warps: the two longest buckets of symmetric units, the medium one-sided units, the rest of
+  // the symmetric units
+  auto warp_sym = [&](int b0, int b1) {
+    if constexpr (EQM) {
+      if (!sym_on) return;
+      for (int b = b0; b < b1; ++b) {
+        const u32 cnt = __ldcg(&counter[SLOT_SYM_COUNT + b]), off = sym_bucket_start(counter, b);
+        for (;;) {
+          u32 m = 0;
+          if (lane == 0) m = atomicAdd(&counter[SLOT_SYM_TAKEN + b], 1u);
+          m = __shfl_sync(0xFFFFFFFFu, m, 0);
+          if (m >= cnt) break;
+          sym_unit<EXACT, false>(c, sym_slots, __ldg(&sym_units[off + m]), jbuf, part, tab_base, lane, warp);
+        }
+      }
+    }
+  };
+  warp_sym(SYM_NB_CTA, SYM_NB_CTA + 2);
   for (;;) {
     u32 m = 0;
     if (lane == 0) m = atomicAdd(&counter[1], 1u);
@@ -572,6 +970,7 @@ __global__ void __maxnreg__(128) pair_slot_kernel(
     if (m >= nmedium) break;
     slot_unit<EQM, EXACT, false>(c, __ldg(&heavy[heavy_cap - 1 - m]), jbuf, part, tab_base, lane, warp);
   }
+  warp_sym(SYM_NB_CTA + 2, SYM_NB);
   for (;;) {
     u32 it = 0;
     if (lane == 0) it = atomicAdd(&counter[8], 1u);
@@ -583,23 +982,53 @@ __global__ void __maxnreg__(128) pair_slot_kernel(
   }
 }
 
-// Sum of the 27 slots in slot order (Kahan), plus the PM acceleration; in a run the kick, the
-// drift, the unit round trip and the escape test, writing the new state to the other buffers.
+// Sum of the 27 slots in slot order (Kahan), each direction's one-sided slot followed by its
+// symmetric slots in sub-column order (when the pass had a symmetric part: sym_slots non-null and
+// the unit list complete), plus the PM acceleration; in a run the kick, the drift, the unit round
+// trip and the escape test, writing the new state to the other buffers.
 __global__ void __launch_bounds__(256) pair_epilogue_kernel(
     const float4* __restrict__ pm, const float4* __restrict__ vi, const float4* __restrict__ acc_pm,
     const float4* __restrict__ slots, int n, StepParams sp, float kick, int drift, int kdk,
     float4* __restrict__ pm_out, float4* __restrict__ vi_out, float4* __restrict__ acc_out,
-    int* stop) {
+    const float4* __restrict__ sym_slots, const u32* __restrict__ sym_masks, const int* __restrict__ subcol,
+    const u32* __restrict__ counter, u32 sym_cap, int* stop) {
   if (stopped_before(stop, kdk && drift, sp.step_tag)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+  if (sym_slots && __ldcg(&counter[SLOT_SYM_TOTAL]) <= sym_cap) {
+    const u32* mw = sym_masks + (size_t)subcol[i] * SYM_MASK_WORDS;
+    u32 w[SYM_MASK_WORDS];
+#pragma unroll
+    for (int t = 0; t < SYM_MASK_WORDS; ++t) w[t] = mw[t];
+#pragma unroll
+    for (int k = 0; k < NNB; ++k) {
+      const float4 v = slots[(size_t)k * n + i];
+      kahan_add(sx, cx, v.x);
+      kahan_add(sy, cy, v.y);
+      kahan_add(sz, cz, v.z);
+      // bits 9k .. 9k + 8 (constants once k is unrolled)
+      const int lo = k * SYM_LOCAL, t = lo >> 5, off = lo & 31;
+      u32 field = w[t] >> off;
+      if (off + SYM_LOCAL > 32) field |= w[t + 1] << (32 - off);
+      field &= (1u << SYM_LOCAL) - 1u;
+      while (field) {
+        const int q = __ffs(field) - 1;
+        field &= field - 1u;
+        const float4 e = sym_slots[(size_t)(lo + q) * n + i];
+        kahan_add(sx, cx, e.x);
+        kahan_add(sy, cy, e.y);
+        kahan_add(sz, cz, e.z);
+      }
+    }
+  } else {
 #pragma unroll 9
-  for (int k = 0; k < NNB; ++k) {
-    const float4 v = slots[(size_t)k * n + i];
-    kahan_add(sx, cx, v.x);
-    kahan_add(sy, cy, v.y);
-    kahan_add(sz, cz, v.z);
+    for (int k = 0; k < NNB; ++k) {
+      const float4 v = slots[(size_t)k * n + i];
+      kahan_add(sx, cx, v.x);
+      kahan_add(sy, cy, v.y);
+      kahan_add(sz, cz, v.z);
+    }
   }
   const float4 ap = acc_pm[i];
   const float3 a = make_float3(ap.x + sx, ap.y + sy, ap.z + sz);
@@ -637,8 +1066,9 @@ __global__ void item_build_kernel(const int* __restrict__ cell_start, const u32*
 
 // counter words of the table pass: [0] heavy units taken (by CTAs), [1] medium units taken,
 // [2] heavy units listed, [3] medium units listed, [4..5] u64 total estimated cost, [6..7] u64
-// heavy threshold, [8] other units taken.
-constexpr int SLOT_COUNTER_WORDS = 10;
+// heavy threshold, [8] other units taken, [10, 19) symmetric units per cost bucket, [19, 28) taken
+// per bucket, [28] symmetric units listed.
+constexpr int SLOT_COUNTER_WORDS = 32;
 
 // Total estimated cost of all units (one thread per item, its 27 neighbour cells).
 __global__ void plan_cost_kernel(const int* __restrict__ cell_start, const int2* __restrict__ items,
@@ -714,6 +1144,13 @@ int slot_heavy_capacity(int nitems_max) {
   return (int)(units < (1 << 22) ? units : (1 << 22));
 }
 
+// Units a symmetric pass can list: up to 125 per sub-column of at least SYM_MIN_SMALL particles
+// (13 x 9 upper-half neighbours and 8 within the cell), at most 2^24.
+int sym_unit_capacity(int nsub, int n) {
+  const long long units = 125LL * (long long)std::max(std::min(nsub, n / SYM_MIN_SMALL), 1);
+  return (int)(units < (1 << 24) ? units : (1 << 24));
+}
+
 int exclusive_scan(const u32* in, u32* out, int n, u32* total, u32* scratch, cudaStream_t st);
 
 int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const int* cell_start,
@@ -721,7 +1158,8 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
                 int nitems_max, u32* heavy, u32* counter, const PairParams& pp, const float* table,
                 const StepParams& sp, float kick, int drift, int kdk, float4* pm_out, float4* vi_out,
                 float4* acc_out, unsigned long long* npairs, int* stop, int num_sms, cudaEvent_t ev_pair,
-                cudaStream_t st, int equal_mass, float4* slots, int n, int unit_stride) {
+                cudaStream_t st, int equal_mass, float4* slots, int n, int unit_stride,
+                const SymPass* sym) {
   const u32 ustride = unit_stride > 1 ? (u32)unit_stride : 1u;
   const int ncells = chd.Mx * chd.My * chd.Mz;
   const int ntot = ncells * chd.sub * chd.sub + 1;  // sub-columns + the bucket outside the mesh
@@ -729,6 +1167,9 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
   const bool exact = !pp.use_table && pp.eps2 == 0.f;
   const bool slotted = (pp.use_table || exact) && !npairs && slots;
   const int slice = slotted ? SLOT_SLICE : 32;
+  // the symmetric part: equal masses, 3 x 3 y-sorted sub-columns, every slice (not sampled)
+  const bool sym_on = slotted && sym && sym->enabled && sym->slots && equal_mass && chd.sub == 3 &&
+                      pp.ysort && ustride == 1 && nitems_max > 0 && n > 0;
   item_count_kernel<<<(ntot + 255) / 256, 256, 0, st>>>(cell_start, ntot, item_cnt, slice, stop);
   int rc = exclusive_scan(item_cnt, item_off, ntot, nitems, scan_tmp, st);
   if (rc) return rc;
@@ -743,10 +1184,21 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
     plan_heavy_kernel<<<pb, 256, 0, st>>>(cell_start, items, nitems, cd, heavy, heavy_cap, counter,
                                           (unsigned long long)num_sms * SLOT_CTAS_PER_SM * SLOT_WARPS, ustride,
                                           stop);
+    if (sym_on) {
+      const int nsub = ncells * SYM_LOCAL;
+      // units buffer: 2 cap uint2 of staging (as cap uint4), then the laid-out list
+      uint4* stage = reinterpret_cast<uint4*>(sym->units);
+      sym_plan_kernel<<<(nsub + 1 + 255) / 256, 256, 0, st>>>(cell_start, cd, nsub, pp.re2,
+                                                             1e-3f * fminf(cd.HCsx, cd.HCsz), sym->masks,
+                                                             stage, sym->cap, counter, stop);
+      sym_scatter_kernel<<<num_sms * 4, 256, 0, st>>>(stage, sym->units + 2 * (size_t)sym->cap, sym->cap, counter,
+                                                       stop);
+      subcol_kernel<<<pb, 256, 0, st>>>(cell_start, items, nitems, sym->subcol, stop);
+    }
   }
   if (ev_pair) PMGB_CUDA_TRY(cudaEventRecord(ev_pair, st));
   const dim3 grid(num_sms * 8), block(PAIR_THREADS);
-  if (slotted) {  // table, staging and partial sums: 88.1 KB of dynamic shared memory
+  if (slotted) {  // table, staging and partial sums: 104.6 KB of dynamic shared memory
     PMGB_CUDA_TRY(cudaFuncSetAttribute(pair_slot_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SLOT_SMEM));
     PMGB_CUDA_TRY(cudaFuncSetAttribute(pair_slot_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SLOT_SMEM));
     PMGB_CUDA_TRY(cudaFuncSetAttribute(pair_slot_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SLOT_SMEM));
@@ -757,13 +1209,18 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
   int launches = 3;  // item count, item build, pair pass (the scan counts itself)
   if (slotted) {
     if (nitems_max > 0) launches += 2;  // the two planning kernels
+    if (sym_on) launches += 3;  // symmetric planning, unit lay-out, sub-column ids
     auto kern = equal_mass ? (exact ? pair_slot_kernel<true, true> : pair_slot_kernel<true, false>)
                            : (exact ? pair_slot_kernel<false, true> : pair_slot_kernel<false, false>);
     kern<<<num_sms * SLOT_CTAS_PER_SM, SLOT_THREADS, SLOT_SMEM, st>>>(
-        pm, n, cell_start, items, nitems, heavy, heavy_cap, counter, cd, pp, table, slots, ustride, stop);
+        pm, n, cell_start, items, nitems, heavy, heavy_cap, counter, cd, pp, table, slots, ustride,
+        sym_on ? sym->masks : nullptr, sym_on ? sym->cap : 0u, sym_on ? sym->slots : nullptr,
+        sym_on ? sym->units + 2 * (size_t)sym->cap : nullptr, stop);
     if (n > 0)
-      pair_epilogue_kernel<<<(n + 255) / 256, 256, 0, st>>>(pm, vi, acc_pm, slots, n, sp, kick, drift,
-                                                            kdk, pm_out, vi_out, acc_out, stop);
+      pair_epilogue_kernel<<<(n + 255) / 256, 256, 0, st>>>(
+          pm, vi, acc_pm, slots, n, sp, kick, drift, kdk, pm_out, vi_out, acc_out,
+          sym_on ? sym->slots : nullptr, sym_on ? sym->masks : nullptr, sym_on ? sym->subcol : nullptr, counter,
+          sym_on ? sym->cap : 0u, stop);
     ++launches;
   } else if (pp.use_table) {
     if (npairs) pair_kernel<true, true><<<grid, block, 0, st>>>(PMGB_PAIR_ARGS);

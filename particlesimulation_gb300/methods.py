@@ -491,6 +491,16 @@ class P3MMethod:
     def setPairCounting(self, enable: bool):
         check(lib().pmgb_p3m_set_pair_counting(self._h, int(bool(enable))))
 
+    def setSymmetric(self, enable: bool):
+        """Evaluate the light sub-column pairs once (on by default where it applies)."""
+        check(lib().pmgb_p3m_set_symmetric(self._h, int(bool(enable))))
+
+    def symmetric(self):
+        """(switch on, sub-column pairs the last force evaluation took once)."""
+        e, u = C.c_int(0), C.c_uint(0)
+        check(lib().pmgb_p3m_get_symmetric(self._h, C.byref(e), C.byref(u)))
+        return bool(e.value), int(u.value)
+
     def pairCount(self) -> int:
         """Ordered pairs within the cutoff in the last force evaluation."""
         c = C.c_ulonglong(0)

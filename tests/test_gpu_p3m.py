@@ -185,3 +185,74 @@ def test_p3m_dense_cluster_heavy_units(gpu_lib):
     assert rel_rms(acc1[idx], f64) < 1e-5
     p3m.close()
     pm.close()
+
+
+def _sym_case(n, table, seed, grid=64, spread=(0.6, 2.5)):
+    rng = np.random.default_rng(seed)
+    H = 30.0 / (grid // 2)
+    pos = np.concatenate([rng.normal(15.0, spread[0], (n // 2, 3)), rng.normal(15.0, spread[1], (n // 4, 3)),
+                          rng.uniform(4.0, 26.0, (n - n // 2 - n // 4, 3))])
+    pos = np.clip(pos, 4.0, 26.0).astype(np.float32)
+    vel = rng.normal(0, 0.01, (n, 3)).astype(np.float32)
+    mass = np.full(n, 1.0 / n, np.float32)
+    cfg = O.PMConfig(grid=(grid,) * 3, box=(30.0,) * 3, H=H, DT=0.05, G=1.0,
+                     interpolation=2, finite_diff=0, greens=2, diameter=3 * H)
+    q = O.P3MConfig(comp_box=(30.0,) * 3, cutoff=3 * H, diameter=3 * H, softening=0.0,
+                    cloud_shape=1, use_table=table)
+    return cfg, q, pos, vel, mass
+
+
+@pytest.mark.parametrize("table", [1, 0])
+def test_symmetric_pass_matches_one_sided(gpu_lib, table):
+    """The pair pass's symmetric part (light sub-column pairs evaluated once, each side into a
+    slot of its own, summed in a fixed order): it takes a large share of the pairs here, its
+    forces equal the one-sided pass's to float rounding and the FP64 oracle's within the parity
+    bar, and two evaluations are bit-identical (every slot has one writer)."""
+    from conftest import err_stats
+    cfg, q, pos, vel, mass = _sym_case(60000, table, seed=21)
+    pm, p3m = make_p3m(cfg, q, pos, vel, mass)
+    on, _ = p3m.symmetric()
+    assert on
+    p3m.force()
+    acc_sym = pm.getParticles()[2].copy()
+    units = p3m.symmetric()[1]
+    assert units > 50, units
+    p3m.force()
+    np.testing.assert_array_equal(acc_sym, pm.getParticles()[2])
+    p3m.setSymmetric(False)
+    p3m.force()
+    acc_one = pm.getParticles()[2].copy()
+    assert p3m.symmetric() == (False, 0)
+    st = err_stats(acc_sym, acc_one)
+    assert st["rms"] < 1e-6 and st["median"] < 1e-6, st
+    rng = np.random.default_rng(5)
+    idx = np.sort(rng.choice(len(pos), 1500, replace=False)).astype(np.int32)
+    f64 = O.port_p3m_accel_targets(cfg, q, pos, vel, mass, idx, prec=1)
+    e_sym, e_one = rel_rms(acc_sym[idx], f64), rel_rms(acc_one[idx], f64)
+    if table:
+        assert e_sym < 1e-5 and e_one < 1e-5
+    else:
+        # the exact formula's 1/r^2 on the cluster's close pairs magnifies the float rounding of
+        # the positions for both passes alike (the parity bar of the formula is in
+        # test_p3m_table_free_force); the symmetric pass must not add to it
+        assert e_sym <= 1.01 * e_one + 1e-7, (e_sym, e_one)
+    p3m.close()
+    pm.close()
+
+
+def test_symmetric_pass_run_bit_identical(gpu_lib):
+    """A multi-step P3M run with the symmetric part on: repeated runs from the same state give
+    bit-identical particles, and the end state stays within float rounding of the one-sided
+    run's."""
+    cfg, q, pos, vel, mass = _sym_case(30000, 1, seed=23, grid=32, spread=(1.0, 3.0))
+    outs = []
+    for sym in (True, True, False):
+        pm, p3m = make_p3m(cfg, q, pos, vel, mass)
+        p3m.setSymmetric(sym)
+        escaped, steps = p3m.run(5)
+        assert not escaped and steps == 6
+        outs.append(pm.getParticles(units="original")[0].copy())
+        p3m.close()
+        pm.close()
+    np.testing.assert_array_equal(outs[0], outs[1])
+    assert np.abs(outs[0] - outs[2]).max() < 1e-5 * np.abs(outs[2]).max()
