@@ -264,8 +264,8 @@ constexpr int SYM_LOCAL = 9;
 constexpr int SYM_NSLOT = NNB * SYM_LOCAL;
 constexpr int SYM_MASK_WORDS = (SYM_NSLOT + 31) / 32;
 // counter words of the slotted pass (see SLOT_COUNTER_WORDS)
-// symmetric units in cost buckets (longest first): 0..3 for CTAs (|p| |q| >= 8, 2, 1/2, 1/4
-// heavy thresholds), 4..8 for warps (>= 1/8, 1/16, 1/32, 1/64 of the threshold, below)
+// symmetric units in cost buckets (longest first): 0..3 for CTAs (|p| |q| >= 8, 2, 1, 1/2 heavy
+// thresholds), 4..8 for warps (>= 1/4, 1/8, 1/16, 1/32 of the threshold, below)
 constexpr int SYM_NB = 9, SYM_NB_CTA = 4;
 constexpr int SLOT_SYM_COUNT = 10, SLOT_SYM_TAKEN = SLOT_SYM_COUNT + SYM_NB, SLOT_SYM_TOTAL = SLOT_SYM_TAKEN + SYM_NB;
 constexpr unsigned long long SLOT_HEAVY_MIN = 64ull * 1024;
@@ -531,7 +531,7 @@ __device__ __forceinline__ void slot_unit(const SlotCtx& c, u32 it, float4 (*jbu
 //     and 3, so that every lane sends and keeps the same registers), each lane keeping one
 //     candidate's total per chunk of 32, added to the slot (cleared at the unit's start;
 //     read-modify-written by one warp at a time, in slice order).
-// Units of cost |p| |q| >= 1/4 of the heavy threshold are taken by whole CTAs (the warps split each
+// Units of cost |p| |q| >= 1/2 of the heavy threshold are taken by whole CTAs (the warps split each
 // window's chunks, the i sides added in warp order through shared memory), the rest by warps.
 // Every slot has one writer at a time and a fixed summation order: the result is deterministic.
 // The one-sided pass skips the pairs marked in the sub-column's mask and the epilogue adds the
@@ -540,7 +540,7 @@ __device__ __forceinline__ void slot_unit(const SlotCtx& c, u32 it, float4 (*jbu
 constexpr int SYM_IPL = 4;                // i particles per lane
 constexpr int SYM_SLICE = 32 * SYM_IPL;   // particles per slice of a unit's i side
 constexpr int SYM_MIN_BIG = 128;          // the larger list of a symmetric pair, at least
-constexpr int SYM_MIN_SMALL = 16;         // the smaller one, at least
+constexpr int SYM_MIN_SMALL = 8;          // the smaller one, at least
 constexpr unsigned long long SYM_CTA_MUL = 16;  // |p| |q| below 16 heavy thresholds
 
 struct SymI {
@@ -565,8 +565,8 @@ __device__ __forceinline__ float sym_gap2(const ChainDimsP& cd, int gx, int gz, 
 // the buckets out one after the other in units.  If more than cap units are listed, the pass
 // runs one-sided.
 __device__ __forceinline__ int sym_bucket(unsigned long long c, unsigned long long thr) {
-  if (4 * c >= thr) return c >= 8 * thr ? 0 : c >= 2 * thr ? 1 : 2 * c >= thr ? 2 : 3;
-  return 8 * c >= thr ? 4 : 16 * c >= thr ? 5 : 32 * c >= thr ? 6 : 64 * c >= thr ? 7 : 8;
+  if (2 * c >= thr) return c >= 8 * thr ? 0 : c >= 2 * thr ? 1 : c >= thr ? 2 : 3;
+  return 4 * c >= thr ? 4 : 8 * c >= thr ? 5 : 16 * c >= thr ? 6 : 32 * c >= thr ? 7 : 8;
 }
 
 __global__ void sym_plan_kernel(const int* __restrict__ cs, ChainDimsP cd, int nsub, float re2, float margin,
