@@ -294,9 +294,11 @@ int pmgb_p3m_pair_count(pmgb_p3m* p3m, unsigned long long* ordered_pairs);
  * costs a few percent of the pair pass). */
 int pmgb_p3m_set_pair_counting(pmgb_p3m* p3m, int enable);
 /* Each pair once, as the reference's half-shell pass (source/p3mMethod.cpp:247-273, 296-322)
- * does: with y-sorted lists and equal masses the pair pass evaluates the sub-column pairs that
- * one warp can take whole once, writing both particles' partial forces to slots of their own,
- * and the rest from both sides.  On by default where it applies; off evaluates every pair from
+ * does: with y-sorted lists and equal masses the pair pass evaluates the dense sub-column pairs
+ * below a cost bound (each taken whole by one warp or CTA) once, writing both particles' partial
+ * forces to slots of their own, and the rest from both sides.  On by default where it applies (its slots take 3.9 KB per
+ * particle, allocated with the handle when that is at most a quarter of the free device memory;
+ * otherwise the handle stays one-sided and enable has no effect); off evaluates every pair from
  * both sides.  Both are deterministic; they differ by float rounding.  units_last_pass
  * (may be NULL): the sub-column pairs the last force evaluation took once (0 when it ran
  * one-sided).  No reference counterpart (a switch of this implementation). */
