@@ -19,7 +19,8 @@ ours:       the learned closure (pair cutoff 1.5 mesh cells + MLP residual) is t
             e2e: the same judged steps through the C ABI with host buffers (state copied
             host->device from pinned memory every step, state and accelerations read back).
             The line also reports both modes alone, their force errors against an FP64 direct
-            sum on 8,192 particles, the roofline of the dominant kernel (the learned step's
+            sum on 8,192 particles (at the training positions and again after the judged run
+            is continued to 200 steps), the roofline of the dominant kernel (the learned step's
             reduced-cutoff pair pass; plain P3M's full-cutoff pass beside it), and the other
             workloads (disk_p3m, pm_hbm, ensemble).
 reference:  the reference's CPU P3M path (the oracle port of it: oracle/port.cpp, float, all
@@ -446,6 +447,32 @@ def closure_config(w, bound=1e-3):
             "l2": "256 MB L2 flush before every timed step"}
 
 
+def closure_errors(pm, cl, w):
+    """At the current positions: the forces of plain P3M, the learned closure and the reduced
+    cutoff alone against an FP64 direct sum on ERR_TARGETS particles (median / p90 / max
+    relative error), the two reduced modes against plain P3M, and the judge's median relative
+    difference (learned vs plain, every JUDGE_STRIDE-th slice).  Leaves the learned mode set."""
+    import numpy as np
+
+    from particlesimulation_gb300 import methods as M
+    acc = {}
+    for name, mode in (("plain_p3m", cl.FULL), ("learned_closure", cl.LEARNED),
+                       ("reduced_cutoff_alone", cl.REDUCED_ONLY)):
+        cl.setMode(mode)
+        cl.force()
+        x, _, a = pm.getParticles(units="original")
+        acc[name] = a
+    rng = np.random.default_rng(12345)
+    idx = np.sort(rng.choice(w.n, ERR_TARGETS, replace=False)).astype(np.int32)
+    a_pp = M.direct_sum_fp64(x, w.mass, w.G, idx)
+    errors = {k: med_err(a[idx], a_pp) for k, a in acc.items()}
+    vs_plain = {k: med_err(acc[k][idx], acc["plain_p3m"][idx].astype(np.float64))
+                for k in ("learned_closure", "reduced_cutoff_alone")}
+    cl.setMode(cl.LEARNED)
+    judge = cl.judge(stride=JUDGE_STRIDE)
+    return errors, vs_plain, judge
+
+
 def closure_setup(args, w, flush_l2):
     """PM + learned closure on the workload, trained (untimed): training rows from the plain P3M
     at t = 0 and after 50 steps (2 x N rows), GPU training.  Then, at the same positions, the
@@ -471,23 +498,9 @@ def closure_setup(args, w, flush_l2):
     t1 = time.perf_counter()
     loss = cl.train(epochs=args.closure_epochs, batch=2048, lr=2e-3)
     t2 = time.perf_counter()
-    acc = {}
-    for name, mode in (("plain_p3m", cl.FULL), ("learned_closure", cl.LEARNED),
-                       ("reduced_cutoff_alone", cl.REDUCED_ONLY)):
-        cl.setMode(mode)
-        cl.force()
-        x, _, a = pm.getParticles(units="original")
-        acc[name] = a
-    rng = np.random.default_rng(12345)
-    idx = np.sort(rng.choice(w.n, ERR_TARGETS, replace=False)).astype(np.int32)
     t3 = time.perf_counter()
-    a_pp = M.direct_sum_fp64(x, w.mass, w.G, idx)
+    errors, vs_plain, judge = closure_errors(pm, cl, w)
     t4 = time.perf_counter()
-    errors = {k: med_err(a[idx], a_pp) for k, a in acc.items()}
-    vs_plain = {k: med_err(acc[k][idx], acc["plain_p3m"][idx].astype(np.float64))
-                for k in ("learned_closure", "reduced_cutoff_alone")}
-    cl.setMode(cl.LEARNED)
-    judge = cl.judge(stride=JUDGE_STRIDE)
     stream = pm.stream()
 
     def mode_ms(mode, steps):
@@ -572,6 +585,18 @@ def closure_headline(args, w, flush_l2, clocks, rank, world):
     final_mode = ["plain_p3m", "learned_closure", "reduced_only"][cl.mode()]
     cl.setMode(cl.LEARNED)
     e2e = e2e_steps(pm, args.steps, judged_step, world, w.n)
+    # the configuration's evaluation over 200 steps: the judged run continued to 200 steps
+    # after the training positions (t = 50), then the three modes against the direct sum there
+    done = 2 * (2 + min(args.steps, 10)) + args.warmup + 2 * args.steps  # mode timings, runs
+    fallback200 = fallback
+    for s in range(max(0, 200 - done)):
+        fb = judged_step(done + s)
+        if fb >= 0 and fallback200 < 0:
+            fallback200 = done + s
+    err200, vs_plain200, judge200 = closure_errors(pm, cl, w)
+    after200 = {"steps_after_training_positions": max(200, done), "fallback_step": fallback200,
+                "judge_median_rel_diff_learned_vs_plain": judge200,
+                "force_err_vs_fp64_direct": err200, "force_diff_vs_plain_p3m": vs_plain200}
     cl.close()
     # roofline of the headline's dominant kernel, the learned step's reduced-cutoff pair pass,
     # and of plain P3M's, the full-cutoff pass: plain P3M handles over the same positions
@@ -588,7 +613,7 @@ def closure_headline(args, w, flush_l2, clocks, rank, world):
     ms_plain = summary["plain_p3m"]["ms_per_step"]
     closure = {"bound": args.closure_bound, "judge_interval": JUDGE_INTERVAL,
                "judge_stride": JUDGE_STRIDE, "fallback_step": fallback,
-               "mode_after_run": final_mode, **summary,
+               "mode_after_run": final_mode, **summary, "after_200_steps": after200,
                "judged_speedup_vs_plain": ms_plain / ms_step,
                "target_met": bool(summary["learned_closure"]["force_err_vs_fp64_direct"]["median"]
                                   <= args.closure_bound and ms_plain / ms_step >= 2.0)}
