@@ -509,12 +509,6 @@ __device__ __forceinline__ void slot_unit(const SlotCtx& c, u32 it, float4 (*jbu
   }
 }
 
-// The heavy units listed by plan_heavy_kernel (heavy[0, counter[2]), cost at least the
-// threshold thr in counter[6..7]) are taken first, each by a whole CTA (counter[0]), so that
-// no single warp is left with a unit of tens of thousands of candidates per particle while the
-// others idle; then every warp takes the medium units (cost in [thr / 4, thr), listed from the
-// far end of the same buffer, counter[1]), then the rest in unit order (counter[8]).  If the
-// lists overflowed the buffer, every unit is taken by the last loop.
 // ------------------------------------------------ symmetric sub-column pairs ------------
 // The reference evaluates each pair once (half shell of 13 neighbour cells, the j side written
 // to per-neighbour slots of j: source/p3mMethod.cpp:247-273, 296-322).  Here the same holds for
@@ -891,6 +885,16 @@ __device__ __forceinline__ void slot_table_setup(const float4* __restrict__ pm, 
   cn_out = cn;
 }
 
+// The slotted pass, one persistent CTA per SM.  The heavy one-sided units listed by
+// plan_heavy_kernel (heavy[0, counter[2]), cost at least the threshold thr in counter[6..7]) are
+// taken first, each by a whole CTA (counter[0]), so that no single warp is left with a unit of
+// tens of thousands of candidates per particle while the others idle; then (equal masses, when
+// the symmetric part is on) the symmetric units of CTAs, longest bucket first; then every warp
+// takes the two longest buckets of symmetric warp units, the medium one-sided units (cost in
+// [thr / 4, thr), listed from the far end of the heavy buffer, counter[1]), the other symmetric
+// units, and the rest of the one-sided units in unit order (counter[8]).  If the heavy lists
+// overflowed their buffer, every one-sided unit is taken by the last loop; if the symmetric
+// list overflowed, the pass is one-sided.
 template <bool EQM, bool EXACT>
 __global__ void __maxnreg__(128) pair_slot_kernel(
     const float4* __restrict__ pm, int n, const int* __restrict__ cell_start,
