@@ -722,13 +722,13 @@ int p3m_create_internal(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out,
     return rc;
   }
   // the symmetric part of the pair pass (y-sorted 3 x 3 sub-columns): 243 slots per particle
-  // (3.9 KB), 8 mask words per sub-column, the unit list; left off if it would take more than a
+  // (3.9 KB), the mask words per sub-column, the unit list; left off if it would take more than a
   // quarter of the free device memory or the allocation fails
   if (q->cd.sub == 3 && pm->n > 0) {
     const size_t n = (size_t)pm->n;
     q->sym.cap = (u32)sym_unit_capacity(q->nsub, pm->n);
     void* ptr[4] = {nullptr, nullptr, nullptr, nullptr};
-    const size_t bytes[4] = {243 * n * sizeof(float4), ((size_t)q->nsub + 1) * 8 * sizeof(u32),
+    const size_t bytes[4] = {243 * n * sizeof(float4), ((size_t)q->nsub + 1) * sym_mask_words() * sizeof(u32),
                              3 * (size_t)q->sym.cap * sizeof(uint2), n * sizeof(int)};
     size_t free_b = 0, total_b = 0;
     bool ok = cudaMemGetInfo(&free_b, &total_b) == cudaSuccess &&

@@ -52,13 +52,14 @@ int launch_pack(const float* pos, const float* vel, const float* mass_code, int 
 // (direction, neighbour sub-column); the rest stays one-sided.
 struct SymPass {
   float4* slots = nullptr;  // 243 x n partial accelerations, slot = direction * 9 + sub-column
-  u32* masks = nullptr;     // 8 words per sub-column (nsub + 1): which slots the pass used
+  u32* masks = nullptr;     // sym_mask_words() per sub-column (nsub + 1): slots used, dead directions
   uint2* units = nullptr;   // 3 cap: staged units (cap x 16 B), then the list (i side, j side)
   u32 cap = 0;              // units a pass can list
   int* subcol = nullptr;    // sub-column of each particle (sorted order)
   int enabled = 0;          // the handle's switch (pmgb_p3m_set_symmetric)
 };
 int sym_unit_capacity(int nsub, int n);
+int sym_mask_words();  // mask words per sub-column
 
 int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const int* cell_start,
                 const ChainDims& cd, u32* item_cnt, u32* item_off, u32* scan_tmp, u32* nitems, int2* items,

@@ -258,11 +258,15 @@ constexpr int SLOT_SMEM = SLOT_WARPS * 32 * 16 + SLOT_WARPS * SLOT_PART * 16 + S
 // Units whose estimated cost reaches 1/SLOT_HEAVY_DIV of a warp's share of the pass (and at
 // least SLOT_HEAVY_MIN) are taken by whole CTAs.
 constexpr int SLOT_HEAVY_DIV = 4;
+constexpr int SLOT_REST_BATCH = 1;  // one-sided units a warp claims per fetch in the last loop (4: -1 % on
+                                     // the reduced pass, +1 % elsewhere; 32: +3-5 %)
 // symmetric sub-column pairs: 3 x 3 sub-columns per cell, one slot per (direction, neighbour
 // sub-column) and particle, 243 bits of which per sub-column
 constexpr int SYM_LOCAL = 9;
 constexpr int SYM_NSLOT = NNB * SYM_LOCAL;
-constexpr int SYM_MASK_WORDS = (SYM_NSLOT + 31) / 32;
+// mask words per sub-column: 243 mark bits, then one word of dead directions (bit k: nothing
+// one-sided is left toward neighbour cell k)
+constexpr int SYM_MARK_WORDS = (SYM_NSLOT + 31) / 32, SYM_MASK_WORDS = SYM_MARK_WORDS + 1;
 // counter words of the slotted pass (see SLOT_COUNTER_WORDS)
 // symmetric units in cost buckets (longest first): 0..3 for CTAs (|p| |q| >= 8, 2, 1, 1/2 heavy
 // thresholds), 4..8 for warps (>= 1/4, 1/8, 1/16, 1/32 of the threshold, below)
@@ -554,6 +558,21 @@ __device__ __forceinline__ float sym_gap2(const ChainDimsP& cd, int gx, int gz, 
   return __fadd_rn(__fmul_rn(gxs, gxs), __fmul_rn(gzs, gzs));
 }
 
+// The 9 mark bits of direction k (bits 9k .. 9k + 8) in the mask words w.
+__device__ __forceinline__ u32 sym_field(const u32 (&w)[SYM_MASK_WORDS], int k) {
+  const int lo = k * SYM_LOCAL, t = lo >> 5, off = lo & 31;
+  u32 field = w[t] >> off;
+  if (off + SYM_LOCAL > 32 && t + 1 < SYM_MARK_WORDS) field |= w[t + 1] << (32 - off);
+  return field & ((1u << SYM_LOCAL) - 1u);
+}
+
+// True if nothing one-sided is left between sub-column a and neighbour cell k (every one of its
+// sub-columns empty, out of reach in x-z or taken by the symmetric units): the one-sided unit is
+// skipped and its slot not read.
+__device__ __forceinline__ bool sym_dead(const u32* __restrict__ masks, int a, int k) {
+  return (__ldg(&masks[(size_t)a * SYM_MASK_WORDS + SYM_MARK_WORDS]) >> k) & 1u;
+}
+
 // Marks and units, one thread per sub-column a (a = nsub: the bucket outside the mesh, no marks).
 // Each unit is staged as (p, q, bucket, position in its bucket); sym_scatter_kernel then lays
 // the buckets out one after the other in units.  If more than cap units are listed, the pass
@@ -577,19 +596,29 @@ __global__ void sym_plan_kernel(const int* __restrict__ cs, ChainDimsP cd, int n
     const unsigned long long thr = __ldcg(reinterpret_cast<const unsigned long long*>(counter + 6));
     const int cell = a / SYM_LOCAL, ca = a % SYM_LOCAL;
     const int gx = cell % cd.Mx, gy = (cell / cd.Mx) % cd.My, gz = cell / (cd.Mx * cd.My);
+    u32 dead = 0u;
     for (int k = 0; k < NNB; ++k) {
       const int nx = gx + k % 3 - 1, ny = gy + (k / 3) % 3 - 1, nz = gz + k / 9 - 1;
-      if (nx < 0 || ny < 0 || nz < 0 || nx >= cd.Mx || ny >= cd.My || nz >= cd.Mz) continue;
+      if (nx < 0 || ny < 0 || nz < 0 || nx >= cd.Mx || ny >= cd.My || nz >= cd.Mz) {
+        dead |= 1u << k;
+        continue;
+      }
       const int nb = nx + ny * cd.Mx + nz * cd.Mx * cd.My;
+      bool alive = false;  // something one-sided left toward this neighbour cell
 #pragma unroll
       for (int cb = 0; cb < SYM_LOCAL; ++cb) {
         const int b = nb * SYM_LOCAL + cb;
-        if (b == a) continue;
+        if (b == a) {
+          alive = true;
+          continue;
+        }
         const int pb = __ldg(&cs[b + 1]) - __ldg(&cs[b]);
-        if (pb < SYM_MIN_SMALL || max(pa, pb) < SYM_MIN_BIG) continue;
+        if (pb == 0 || sym_gap2(cd, gx, gz, ca, nx, nz, cb, margin) >= re2) continue;
         const unsigned long long cost = (unsigned long long)pa * (unsigned long long)pb;
-        if (cost >= thr * SYM_CTA_MUL) continue;
-        if (sym_gap2(cd, gx, gz, ca, nx, nz, cb, margin) >= re2) continue;
+        if (pb < SYM_MIN_SMALL || max(pa, pb) < SYM_MIN_BIG || cost >= thr * SYM_CTA_MUL) {
+          alive = true;
+          continue;
+        }
         const int sb = k * SYM_LOCAL + cb;
 #pragma unroll
         for (int i = 0; i < SYM_MASK_WORDS; ++i)
@@ -602,7 +631,9 @@ __global__ void sym_plan_kernel(const int* __restrict__ cs, ChainDimsP cd, int n
             stage[idx] = pa >= pb ? make_uint4((u32)a, (u32)b, (u32)bk, pos) : make_uint4((u32)b, (u32)a, (u32)bk, pos);
         }
       }
+      if (!alive) dead |= 1u << k;
     }
+    w[SYM_MARK_WORDS] = dead;
   }
 #pragma unroll
   for (int i = 0; i < SYM_MASK_WORDS; ++i) masks[(size_t)a * SYM_MASK_WORDS + i] = w[i];
@@ -975,14 +1006,19 @@ __global__ void __maxnreg__(128) pair_slot_kernel(
     slot_unit<EQM, EXACT, false>(c, __ldg(&heavy[heavy_cap - 1 - m]), jbuf, part, tab_base, lane, warp);
   }
   warp_sym(SYM_NB_CTA + 2, SYM_NB);
+  // the rest, SLOT_REST_BATCH units per fetch: each lane tests one (sampled slice, not listed,
+  // not a dead direction of the symmetric part) and the warp runs the live ones in unit order
   for (;;) {
-    u32 it = 0;
-    if (lane == 0) it = atomicAdd(&counter[8], 1u);
-    it = __shfl_sync(0xFFFFFFFFu, it, 0);
-    if (it >= nall) break;
-    if ((it / NNB) % unit_stride) continue;  // sampled pass: every unit_stride-th slice only
-    if (listed && slot_cost(cell_start, cd, items[it / NNB], (int)(it % NNB)) >= thr / 4) continue;
-    slot_unit<EQM, EXACT, false>(c, it, jbuf, part, tab_base, lane, warp);
+    u32 base = 0;
+    if (lane == 0) base = atomicAdd(&counter[8], (u32)SLOT_REST_BATCH);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if (base >= nall) break;
+    const u32 it = base + lane;
+    bool live = lane < SLOT_REST_BATCH && it < nall && (it / NNB) % unit_stride == 0;  // sampled: every stride-th slice
+    if (live && listed) live = slot_cost(cell_start, cd, items[it / NNB], (int)(it % NNB)) < thr / 4;
+    if (live && c.sym_masks) live = !sym_dead(c.sym_masks, items[it / NNB].x, (int)(it % NNB));
+    for (u32 m = __ballot_sync(0xFFFFFFFFu, live); m; m &= m - 1)
+      slot_unit<EQM, EXACT, false>(c, base + (u32)(__ffs(m) - 1), jbuf, part, tab_base, lane, warp);
   }
 }
 
@@ -1007,15 +1043,16 @@ __global__ void __launch_bounds__(256) pair_epilogue_kernel(
     for (int t = 0; t < SYM_MASK_WORDS; ++t) w[t] = mw[t];
 #pragma unroll
     for (int k = 0; k < NNB; ++k) {
-      const float4 v = slots[(size_t)k * n + i];
-      kahan_add(sx, cx, v.x);
-      kahan_add(sy, cy, v.y);
-      kahan_add(sz, cz, v.z);
-      // bits 9k .. 9k + 8 (constants once k is unrolled)
-      const int lo = k * SYM_LOCAL, t = lo >> 5, off = lo & 31;
-      u32 field = w[t] >> off;
-      if (off + SYM_LOCAL > 32) field |= w[t + 1] << (32 - off);
-      field &= (1u << SYM_LOCAL) - 1u;
+      // bits 9k .. 9k + 8 (constants once k is unrolled); a dead direction has no one-sided
+      // slot (its units were skipped)
+      u32 field = sym_field(w, k);
+      const int lo = k * SYM_LOCAL;
+      if (!((w[SYM_MARK_WORDS] >> k) & 1u)) {
+        const float4 v = slots[(size_t)k * n + i];
+        kahan_add(sx, cx, v.x);
+        kahan_add(sy, cy, v.y);
+        kahan_add(sz, cz, v.z);
+      }
       while (field) {
         const int q = __ffs(field) - 1;
         field &= field - 1u;
@@ -1150,6 +1187,8 @@ int slot_heavy_capacity(int nitems_max) {
 
 // Units a symmetric pass can list: up to 125 per sub-column of at least SYM_MIN_SMALL particles
 // (13 x 9 upper-half neighbours and 8 within the cell), at most 2^24.
+int sym_mask_words() { return SYM_MASK_WORDS; }
+
 int sym_unit_capacity(int nsub, int n) {
   const long long units = 125LL * (long long)std::max(std::min(nsub, n / SYM_MIN_SMALL), 1);
   return (int)(units < (1 << 24) ? units : (1 << 24));
