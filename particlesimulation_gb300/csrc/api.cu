@@ -851,8 +851,7 @@ int pmgb_p3m_get_symmetric(pmgb_p3m* q, int* enabled, unsigned int* units_last_p
   if (!q || !enabled) return set_error("null argument"), PMGB_EINVAL;
   *enabled = q->sym.enabled;
   if (units_last_pass) {
-    // counter word 28 of the slotted pass: the symmetric units it listed
-    PMGB_CUDA_TRY(cudaMemcpyAsync(units_last_pass, q->counter + 28, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+    PMGB_CUDA_TRY(cudaMemcpyAsync(units_last_pass, q->counter + kSlotSymTotalWord, sizeof(unsigned int), cudaMemcpyDeviceToHost,
                                   q->pm->st));
     PMGB_CUDA_TRY(cudaStreamSynchronize(q->pm->st));
   }

@@ -59,6 +59,7 @@ struct SymPass {
   int enabled = 0;          // the handle's switch (pmgb_p3m_set_symmetric)
 };
 int sym_unit_capacity(int nsub, int n);
+constexpr int kSlotSymTotalWord = 28;  // counter word of the symmetric units a pass listed
 int sym_mask_words();  // mask words per sub-column
 
 int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const int* cell_start,

@@ -272,6 +272,7 @@ constexpr int SYM_MARK_WORDS = (SYM_NSLOT + 31) / 32, SYM_MASK_WORDS = SYM_MARK_
 // thresholds), 4..8 for warps (>= 1/4, 1/8, 1/16, 1/32 of the threshold, below)
 constexpr int SYM_NB = 9, SYM_NB_CTA = 4;
 constexpr int SLOT_SYM_COUNT = 10, SLOT_SYM_TAKEN = SLOT_SYM_COUNT + SYM_NB, SLOT_SYM_TOTAL = SLOT_SYM_TAKEN + SYM_NB;
+static_assert(SLOT_SYM_TOTAL == kSlotSymTotalWord, "counter layout shared with api.cu");
 constexpr unsigned long long SLOT_HEAVY_MIN = 64ull * 1024;
 
 struct SlotI {
