@@ -256,3 +256,30 @@ def test_symmetric_pass_run_bit_identical(gpu_lib):
         pm.close()
     np.testing.assert_array_equal(outs[0], outs[1])
     assert np.abs(outs[0] - outs[2]).max() < 1e-5 * np.abs(outs[2]).max()
+
+
+def test_symmetric_pass_only_where_it_applies(gpu_lib):
+    """The symmetric part needs equal masses and y-sorted 3 x 3 sub-columns: with unequal masses
+    the pass lists no symmetric unit (and still matches the FP64 oracle), with unsorted cell
+    lists the handle has no symmetric slots at all."""
+    cfg, q, pos, vel, mass = _sym_case(20000, 1, seed=27, grid=32)
+    rng = np.random.default_rng(28)
+    mass = (mass * rng.uniform(0.5, 1.5, len(mass))).astype(np.float32)
+    pm, p3m = make_p3m(cfg, q, pos, vel, mass)
+    p3m.force()
+    assert p3m.symmetric() == (True, 0)
+    idx = np.sort(rng.choice(len(pos), 800, replace=False)).astype(np.int32)
+    f64 = O.port_p3m_accel_targets(cfg, q, pos, vel, mass, idx, prec=1)
+    assert rel_rms(pm.getParticles()[2][idx], f64) < 1e-5
+    p3m.close()
+    pm.close()
+    import particlesimulation_gb300 as P
+    cfg, q, pos, vel, mass = _sym_case(20000, 1, seed=27, grid=32)
+    pm = make_pm(cfg, pos, vel, mass)
+    p3m = P.P3MMethod(pm, q.comp_box, q.cutoff, q.diameter, cfg.H, q.softening,
+                      P.CloudShape(q.cloud_shape), True, False)
+    p3m.setSymmetric(True)
+    p3m.force()
+    assert p3m.symmetric() == (False, 0)
+    p3m.close()
+    pm.close()
