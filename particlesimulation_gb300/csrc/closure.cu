@@ -491,6 +491,29 @@ __device__ __forceinline__ void tc_put(bf16* base, int r, int k, u32 kstride, bf
   *reinterpret_cast<bf16*>(reinterpret_cast<unsigned char*>(base) + canon(r, k, kstride)) = v;
 }
 
+// The training kernel's per-row work goes 16 columns at a time in loops that are not unrolled:
+// the whole epilogue of a layer unrolled runs once per launch, so its straight-line code was
+// always cold in the instruction cache (the kernel spent most of its time on instruction
+// fetch).  Columns k0 .. k0 + 15 of row r of a canonical operand (two 16-byte stores):
+__device__ __forceinline__ void tc_store_row16(bf16* base, int r, int k0, u32 kstride, const float (&v)[16]) {
+  unsigned char* p = reinterpret_cast<unsigned char*>(base);
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    uint4 q;
+    q.x = pack_bf16(v[8 * j + 0], v[8 * j + 1]);
+    q.y = pack_bf16(v[8 * j + 2], v[8 * j + 3]);
+    q.z = pack_bf16(v[8 * j + 4], v[8 * j + 5]);
+    q.w = pack_bf16(v[8 * j + 6], v[8 * j + 7]);
+    *reinterpret_cast<uint4*>(p + canon(r, k0 + 8 * j, kstride)) = q;
+  }
+}
+// rows r0 .. r0 + 15 of column b of a canonical operand whose K dimension is the batch row
+__device__ __forceinline__ void tc_store_col16(bf16* base, int b, int r0, u32 kstride, const float (&v)[16]) {
+  unsigned char* p = reinterpret_cast<unsigned char*>(base);
+#pragma unroll
+  for (int r = 0; r < 16; ++r) *reinterpret_cast<bf16*>(p + canon(r0 + r, b, kstride)) = __float2bfloat16_rn(v[r]);
+}
+
 __global__ void __launch_bounds__(TC_THREADS) closure_train_kernel(
     const bf16* __restrict__ X, const float* __restrict__ T, const int* __restrict__ perm,
     int batch_off, int batch, float inv_batch, const bf16* __restrict__ img,
@@ -544,20 +567,21 @@ __global__ void __launch_bounds__(TC_THREADS) closure_train_kernel(
   const bool valid = row < batch;
   const int src = valid ? perm[batch_off + row] : 0;
   {
-    float f[CL_K0];
     const uint4* xr = reinterpret_cast<const uint4*>(X + (size_t)src * CL_K0);
-#pragma unroll
+#pragma unroll 1
     for (int j = 0; j < CL_K0 / 8; ++j) {
       const uint4 q = valid ? xr[j] : make_uint4(0u, 0u, 0u, 0u);
       *reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(s.x) + canon(tid, 8 * j, TC_KX)) = q;
       const u32 w[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
-      for (int h = 0; h < 4; ++h) {
-        f[8 * j + 2 * h] = __uint_as_float(w[h] << 16);
-        f[8 * j + 2 * h + 1] = __uint_as_float(w[h] & 0xFFFF0000u);
+      for (int h = 0; h < 8; ++h) {  // the input features (rows < CL_IN) of column tid of xt
+        const int r = 8 * j + h;
+        if (r < CL_IN) {
+          const u32 bits = (h & 1) ? (w[h >> 1] >> 16) : (w[h >> 1] & 0xFFFFu);
+          tc_put(s.xt, r, tid, TT_K, __ushort_as_bfloat16((unsigned short)bits));
+        }
       }
     }
-    tc_store_col<CL_IN>(s.xt, tid, TT_K, f);
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -600,13 +624,16 @@ __global__ void __launch_bounds__(TC_THREADS) closure_train_kernel(
       tc_commit(mbar);
     }
     wait();
-    float z[64];
-    tc_ld64(lane + colZ[l], z);
-    const float* b = s.bias + l * CL_H;
+#pragma unroll 1
+    for (int c = 0; c < CL_H / 16; ++c) {
+      float z[16];
+      tc_ld16(lane + colZ[l] + 16u * c, z);
+      const float* b = s.bias + l * CL_H + 16 * c;
 #pragma unroll
-    for (int j = 0; j < 64; ++j) z[j] = gelu(z[j] + b[j]);
-    tc_store_row<CL_H / 8>(reinterpret_cast<unsigned char*>(s.h), tid, TC_KX, z);
-    tc_store_col<CL_H>(s.at[l], tid, TT_K, z);
+      for (int j = 0; j < 16; ++j) z[j] = gelu(z[j] + b[j]);
+      tc_store_row16(s.h, tid, 16 * c, TC_KX, z);
+      tc_store_col16(s.at[l], tid, 16 * c, TT_K, z);
+    }
     publish();
   }
   if (issuer && live) {
@@ -642,29 +669,34 @@ __global__ void __launch_bounds__(TC_THREADS) closure_train_kernel(
   // bias (column bcol; a W column at bcol is the gradient of a zero input and is written 0)
   auto store_dw = [&](u32 col, int rows, int kin, int off_w, int off_b, int bcol) {
     if ((tid & ~31) < rows) {  // whole warps: tcgen05.ld is warp-wide
-      float a[64], c[16];
-      tc_ld64(lane + col, a);
-      tc_ld16(lane + col + 64u, c);
-      if (tid < rows) {
-        float* gr = G + off_w + (size_t)tid * kin;
+      float* gr = G + off_w + (size_t)tid * kin;
+#pragma unroll 1
+      for (int c = 0; c < TT_N / 16; ++c) {
+        float a[16];
+        tc_ld16(lane + col + 16u * c, a);
+        if (tid < rows) {
 #pragma unroll
-        for (int i = 0; i < 64; ++i) gr[i] = (i == bcol) ? 0.f : a[i];
-#pragma unroll
-        for (int i = 64; i < 80; ++i)
-          if (i < kin) gr[i] = (i == bcol) ? 0.f : c[i - 64];
-        G[off_b + tid] = bcol < 64 ? a[bcol & 63] : c[(bcol - 64) & 15];
+          for (int j = 0; j < 16; ++j) {
+            const int i = 16 * c + j;
+            if (i == bcol) G[off_b + tid] = a[j];
+            if (i < kin) gr[i] = (i == bcol) ? 0.f : a[j];
+          }
+        }
       }
     }
   };
   // dZ = dA * GELU'(Z + b) of this row, to dzt (column b) and, when `rows`, to h (row b)
   auto make_dz = [&](u32 col_da, u32 col_z, const float* b, bool rows) {
-    float da[64], z[64];
-    tc_ld64(lane + col_da, da);
-    tc_ld64(lane + col_z, z);
+#pragma unroll 1
+    for (int c = 0; c < CL_H / 16; ++c) {
+      float da[16], z[16];
+      tc_ld16(lane + col_da + 16u * c, da);
+      tc_ld16(lane + col_z + 16u * c, z);
 #pragma unroll
-    for (int j = 0; j < 64; ++j) da[j] *= gelu_grad(z[j] + b[j]);
-    if (rows) tc_store_row<CL_H / 8>(reinterpret_cast<unsigned char*>(s.h), tid, TC_KX, da);
-    tc_store_col<CL_H>(s.dzt, tid, TD_K, da);
+      for (int j = 0; j < 16; ++j) da[j] *= gelu_grad(z[j] + b[16 * c + j]);
+      if (rows) tc_store_row16(s.h, tid, 16 * c, TC_KX, da);
+      tc_store_col16(s.dzt, tid, 16 * c, TD_K, da);
+    }
   };
   auto issue_pair = [&](u32 col_dw, u32 bt, u32 col_da, u32 wt, int nks_da, u32 a_da, u32 akstride, u32 n_da) {
     if (issuer && live) {
