@@ -1186,12 +1186,13 @@ int slot_heavy_capacity(int nitems_max) {
   return (int)(units < (1 << 22) ? units : (1 << 22));
 }
 
-// Units a symmetric pass can list: up to 125 per sub-column of at least SYM_MIN_SMALL particles
-// (13 x 9 upper-half neighbours and 8 within the cell), at most 2^24.
 int sym_mask_words() { return SYM_MASK_WORDS; }
 
+// Units a symmetric pass can list: up to 13 x 9 upper-half neighbours and 8 within the cell per
+// sub-column of at least SYM_MIN_SMALL particles, at most 2^24.
 int sym_unit_capacity(int nsub, int n) {
-  const long long units = 125LL * (long long)std::max(std::min(nsub, n / SYM_MIN_SMALL), 1);
+  constexpr long long per_sub = 13LL * SYM_LOCAL + SYM_LOCAL - 1;
+  const long long units = per_sub * (long long)std::max(std::min(nsub, n / SYM_MIN_SMALL), 1);
   return (int)(units < (1 << 24) ? units : (1 << 24));
 }
 
