@@ -296,14 +296,21 @@ int pmgb_p3m_set_pair_counting(pmgb_p3m* p3m, int enable);
 /* Each pair once, as the reference's half-shell pass (source/p3mMethod.cpp:247-273, 296-322)
  * does: with y-sorted lists and equal masses the pair pass evaluates the dense sub-column pairs
  * below a cost bound (each taken whole by one warp or CTA) once, writing both particles' partial
- * forces to slots of their own, and the rest from both sides.  On by default where it applies (its slots take 3.9 KB per
- * particle, allocated with the handle when that is at most a quarter of the free device memory;
+ * forces to slots of their own, and the rest from both sides.  On by default where it applies (its
+ * slots take 27 s^2 x 16 B per particle, s the sub-columns per cell axis: 3.9, 6.9 or 10.8 KB at
+ * s = 3, 4, 5; allocated with the handle when that is at most a quarter of the free device memory;
  * otherwise the handle stays one-sided and enable has no effect); off evaluates every pair from
  * both sides.  Both are deterministic; they differ by float rounding.  units_last_pass
  * (may be NULL): the sub-column pairs the last force evaluation took once (0 when it ran
  * one-sided).  No reference counterpart (a switch of this implementation). */
 int pmgb_p3m_set_symmetric(pmgb_p3m* p3m, int enable);
 int pmgb_p3m_get_symmetric(pmgb_p3m* p3m, int* enabled, unsigned int* units_last_pass);
+/* Sub-columns per cell axis the pair pass splits each chaining-mesh cell into (x and z): 1 for
+ * the reference's unsorted lists; with y-sorted lists 5 where the handle's particles average at
+ * least 48 per cell (N >= 48 Mx My Mz), 4 from 32, else 3, lowered (not below 3) until the
+ * symmetric slots fit a quarter of the free device memory.  Fixed at creation.  The cell lists
+ * handed out (pmgb_p3m_get_cell_lists) are whole cells either way.  No reference counterpart. */
+int pmgb_p3m_get_subcolumns(const pmgb_p3m* p3m, int* per_axis);
 
 /* ---------------------------------------------------------------- ensemble ----------- */
 /* No counterpart in the reference (one system per process there).  n_systems independent PM

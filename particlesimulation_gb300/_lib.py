@@ -27,7 +27,7 @@ EXPORTS = [
     "pmgb_p3m_force", "pmgb_p3m_run", "pmgb_p3m_get_cell_lists", "pmgb_p3m_get_sr_table",
     "pmgb_p3m_pair_count", "pmgb_fp32_peak_probe", "pmgb_kernel_launches",
     "pmgb_chaining_mesh_fill_noalloc", "pmgb_p3m_set_pair_counting", "pmgb_p3m_set_symmetric",
-    "pmgb_p3m_get_symmetric",
+    "pmgb_p3m_get_symmetric", "pmgb_p3m_get_subcolumns",
     "pmgb_closure_create", "pmgb_closure_destroy", "pmgb_closure_set_mode", "pmgb_closure_get_mode",
     "pmgb_closure_collect", "pmgb_closure_train", "pmgb_closure_param_count",
     "pmgb_closure_get_params", "pmgb_closure_set_params", "pmgb_closure_judge", "pmgb_closure_run",
@@ -119,6 +119,7 @@ def lib() -> C.CDLL:
         L.pmgb_p3m_set_pair_counting.argtypes = [vp, C.c_int]
         L.pmgb_p3m_set_symmetric.argtypes = [vp, C.c_int]
         L.pmgb_p3m_get_symmetric.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_uint)]
+        L.pmgb_p3m_get_subcolumns.argtypes = [vp, C.POINTER(C.c_int)]
         L.pmgb_closure_create.argtypes = [vp, C.POINTER(P3MConfigC), C.c_float, C.c_int,
                                           C.c_ulonglong, C.POINTER(vp)]
         L.pmgb_closure_destroy.argtypes = [vp]

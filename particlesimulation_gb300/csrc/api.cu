@@ -638,10 +638,25 @@ int p3m_create_internal(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out,
   q->cd.HCy = (cfg->comp_box[1] / q->cd.My) / H;
   q->cd.HCz = (cfg->comp_box[2] / q->cd.Mz) / H;
   q->ncells = q->cd.Mx * q->cd.My * q->cd.Mz;
-  // 3 x 3 sub-columns per cell when the lists are y-sorted (the pair pass prunes by x-z gap and
-  // y window per sub-column; 2 x 2 and 4 x 4 measured slower on the disk workloads); the
-  // reference's unsorted fill order keeps whole cells
-  q->cd.sub = cfg->y_sorting ? 3 : 1;
+  // Sub-columns per cell axis when the lists are y-sorted (the pair pass prunes by x-z gap and y
+  // window per sub-column, and its symmetric part pairs sub-columns): 5 where the particles
+  // average at least 48 per cell, 4 from 32, else 3.  Pair pass on the disk workloads, 3 / 4 / 5
+  // sub-columns, by mean particles per cell: 14: 28.0 / 28.4 / 30.3 ms; 28: 6.00 / 6.10 / 6.65;
+  // 39: 47.7 / 44.7 / 45.4; 60: 60.1 / 56.7 / 55.8; 113: 89.4 / 80.2 / 76.5 (2 x 2 was slower
+  // throughout).  A finer split only where its symmetric slots (27 sub^2 x 16 B per particle)
+  // stay within a quarter of the free device memory (the rule the allocation below applies).
+  // The reference's unsorted fill order keeps whole cells.
+  q->cd.sub = 1;
+  if (cfg->y_sorting) {
+    const long long n = pm->n, nc = q->ncells;
+    q->cd.sub = n >= 48 * nc ? 5 : n >= 32 * nc ? 4 : 3;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+      free_b = 0;
+      cudaGetLastError();
+    }
+    while (q->cd.sub > 3 && 27ull * q->cd.sub * q->cd.sub * sizeof(float4) * (size_t)n > free_b / 4) --q->cd.sub;
+  }
   q->cd.HCsx = q->cd.HCx / q->cd.sub;
   q->cd.HCsz = q->cd.HCz / q->cd.sub;
   q->nsub = q->ncells * q->cd.sub * q->cd.sub;
@@ -721,14 +736,14 @@ int p3m_create_internal(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out,
     pmgb_p3m_destroy(q);
     return rc;
   }
-  // the symmetric part of the pair pass (y-sorted 3 x 3 sub-columns): 243 slots per particle
-  // (3.9 KB), the mask words per sub-column, the unit list; left off if it would take more than a
-  // quarter of the free device memory or the allocation fails
-  if (q->cd.sub == 3 && pm->n > 0) {
-    const size_t n = (size_t)pm->n;
-    q->sym.cap = (u32)sym_unit_capacity(q->nsub, pm->n);
+  // the symmetric part of the pair pass (y-sorted lists): 27 sub^2 slots per particle (3.9, 6.9
+  // or 10.8 KB), the mask words per sub-column, the unit list; left off if it would take more
+  // than a quarter of the free device memory or the allocation fails
+  if (sym_supported(q->cd.sub) && pm->n > 0) {
+    const size_t n = (size_t)pm->n, nslot = 27 * (size_t)q->cd.sub * q->cd.sub;
+    q->sym.cap = (u32)sym_unit_capacity(q->nsub, pm->n, q->cd.sub);
     void* ptr[4] = {nullptr, nullptr, nullptr, nullptr};
-    const size_t bytes[4] = {243 * n * sizeof(float4), ((size_t)q->nsub + 1) * sym_mask_words() * sizeof(u32),
+    const size_t bytes[4] = {nslot * n * sizeof(float4), ((size_t)q->nsub + 1) * sym_mask_words(q->cd.sub) * sizeof(u32),
                              3 * (size_t)q->sym.cap * sizeof(uint2), n * sizeof(int)};
     size_t free_b = 0, total_b = 0;
     bool ok = cudaMemGetInfo(&free_b, &total_b) == cudaSuccess &&
@@ -855,6 +870,12 @@ int pmgb_p3m_get_symmetric(pmgb_p3m* q, int* enabled, unsigned int* units_last_p
                                   q->pm->st));
     PMGB_CUDA_TRY(cudaStreamSynchronize(q->pm->st));
   }
+  return PMGB_OK;
+}
+
+int pmgb_p3m_get_subcolumns(const pmgb_p3m* q, int* per_axis) {
+  if (!q || !per_axis) return set_error("null argument"), PMGB_EINVAL;
+  *per_axis = q->cd.sub;
   return PMGB_OK;
 }
 

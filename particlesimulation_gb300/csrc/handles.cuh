@@ -51,16 +51,18 @@ int launch_pack(const float* pos, const float* vel, const float* mass_code, int 
 // bound are evaluated once per pair, each side's partial force going to a slot of its own
 // (direction, neighbour sub-column); the rest stays one-sided.
 struct SymPass {
-  float4* slots = nullptr;  // 243 x n partial accelerations, slot = direction * 9 + sub-column
-  u32* masks = nullptr;     // sym_mask_words() per sub-column (nsub + 1): slots used, dead directions
+  float4* slots = nullptr;  // 27 L x n partial accelerations (L = sub-columns per cell), slot =
+                            // direction * L + sub-column
+  u32* masks = nullptr;     // sym_mask_words(sub) per sub-column (nsub + 1): slots used, dead directions
   uint2* units = nullptr;   // 3 cap: staged units (cap x 16 B), then the list (i side, j side)
   u32 cap = 0;              // units a pass can list
   int* subcol = nullptr;    // sub-column of each particle (sorted order)
   int enabled = 0;          // the handle's switch (pmgb_p3m_set_symmetric)
 };
-int sym_unit_capacity(int nsub, int n);
+int sym_unit_capacity(int nsub, int n, int sub);
 constexpr int kSlotSymTotalWord = 28;  // counter word of the symmetric units a pass listed
-int sym_mask_words();  // mask words per sub-column
+int sym_mask_words(int sub);  // mask words per sub-column with sub x sub sub-columns per cell
+bool sym_supported(int sub);  // sub-column counts the symmetric part is built for
 
 int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const int* cell_start,
                 const ChainDims& cd, u32* item_cnt, u32* item_off, u32* scan_tmp, u32* nitems, int2* items,

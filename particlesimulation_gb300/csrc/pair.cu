@@ -260,13 +260,11 @@ constexpr int SLOT_SMEM = SLOT_WARPS * 32 * 16 + SLOT_WARPS * SLOT_PART * 16 + S
 constexpr int SLOT_HEAVY_DIV = 4;
 constexpr int SLOT_REST_BATCH = 1;  // one-sided units a warp claims per fetch in the last loop (4: -1 % on
                                      // the reduced pass, +1 % elsewhere; 32: +3-5 %)
-// symmetric sub-column pairs: 3 x 3 sub-columns per cell, one slot per (direction, neighbour
-// sub-column) and particle, 243 bits of which per sub-column
-constexpr int SYM_LOCAL = 9;
-constexpr int SYM_NSLOT = NNB * SYM_LOCAL;
-// mask words per sub-column: 243 mark bits, then one word of dead directions (bit k: nothing
-// one-sided is left toward neighbour cell k)
-constexpr int SYM_MARK_WORDS = (SYM_NSLOT + 31) / 32, SYM_MASK_WORDS = SYM_MARK_WORDS + 1;
+// symmetric sub-column pairs: L = sub^2 sub-columns per cell (9, 16 or 25), one slot per
+// (direction, neighbour sub-column) and particle; mask words per sub-column: 27 L mark bits
+// (bit k L + q: neighbour sub-column q of direction k), then one word of dead directions (bit k:
+// nothing one-sided is left toward neighbour cell k)
+__host__ __device__ constexpr int sym_mark_words(int local) { return (NNB * local + 31) / 32; }
 // counter words of the slotted pass (see SLOT_COUNTER_WORDS)
 // symmetric units in cost buckets (longest first): 0..3 for CTAs (|p| |q| >= 8, 2, 1, 1/2 heavy
 // thresholds), 4..8 for warps (>= 1/4, 1/8, 1/16, 1/32 of the threshold, below)
@@ -379,9 +377,10 @@ struct SlotCtx {
   float re2, sc, gap_margin;
   int ysort;
   float cn;  // EXACT: Newton coefficient -G m / re^2 in the scaled coordinates
-  // symmetric part of the pass (null when off): bit k * 9 + q of sub-column a's 8 words marks
-  // neighbour sub-column q of direction k as evaluated by the symmetric units instead
+  // symmetric part of the pass (null when off): bit k sub^2 + q of sub-column a's sym_words
+  // words marks neighbour sub-column q of direction k as evaluated by the symmetric units instead
   const u32* __restrict__ sym_masks;
+  int sym_words;
 };
 
 // One work unit: the slice items[it / 27] against neighbour cell it % 27, into slot k of the
@@ -435,8 +434,8 @@ __device__ __forceinline__ void slot_unit(const SlotCtx& c, u32 it, float4 (*jbu
       const float g2 = gxs * gxs + gzs * gzs;
       if (g2 >= c.re2) continue;
       if (c.sym_masks) {
-        const int sb = k * SYM_LOCAL + qs;
-        if ((__ldg(&c.sym_masks[(size_t)item.x * SYM_MASK_WORDS + (sb >> 5)]) >> (sb & 31)) & 1u) continue;
+        const int sb = k * sub2 + qs;
+        if ((__ldg(&c.sym_masks[(size_t)item.x * c.sym_words + (sb >> 5)]) >> (sb & 31)) & 1u) continue;
       }
       // a pair in range has |dy|^2 < re^2 - (its x-z distance)^2 <= re^2 - g2: the y window
       // of this sub-column is the chord of the cutoff sphere at the sub-column's x-z gap, widened
@@ -559,19 +558,21 @@ __device__ __forceinline__ float sym_gap2(const ChainDimsP& cd, int gx, int gz, 
   return __fadd_rn(__fmul_rn(gxs, gxs), __fmul_rn(gzs, gzs));
 }
 
-// The 9 mark bits of direction k (bits 9k .. 9k + 8) in the mask words w.
-__device__ __forceinline__ u32 sym_field(const u32 (&w)[SYM_MASK_WORDS], int k) {
-  const int lo = k * SYM_LOCAL, t = lo >> 5, off = lo & 31;
+// The L mark bits of direction k (bits k L .. k L + L - 1) in the mask words w.
+template <int L>
+__device__ __forceinline__ u32 sym_field(const u32 (&w)[sym_mark_words(L) + 1], int k) {
+  static_assert(L < 32, "a direction's marks must fit one word");
+  const int lo = k * L, t = lo >> 5, off = lo & 31;
   u32 field = w[t] >> off;
-  if (off + SYM_LOCAL > 32 && t + 1 < SYM_MARK_WORDS) field |= w[t + 1] << (32 - off);
-  return field & ((1u << SYM_LOCAL) - 1u);
+  if (off + L > 32 && t + 1 < sym_mark_words(L)) field |= w[t + 1] << (32 - off);
+  return field & ((1u << L) - 1u);
 }
 
 // True if nothing one-sided is left between sub-column a and neighbour cell k (every one of its
 // sub-columns empty, out of reach in x-z or taken by the symmetric units): the one-sided unit is
 // skipped and its slot not read.
-__device__ __forceinline__ bool sym_dead(const u32* __restrict__ masks, int a, int k) {
-  return (__ldg(&masks[(size_t)a * SYM_MASK_WORDS + SYM_MARK_WORDS]) >> k) & 1u;
+__device__ __forceinline__ bool sym_dead(const u32* __restrict__ masks, int words, int a, int k) {
+  return (__ldg(&masks[(size_t)a * words + words - 1]) >> k) & 1u;
 }
 
 // Marks and units, one thread per sub-column a (a = nsub: the bucket outside the mesh, no marks).
@@ -583,19 +584,21 @@ __device__ __forceinline__ int sym_bucket(unsigned long long c, unsigned long lo
   return 4 * c >= thr ? 4 : 8 * c >= thr ? 5 : 16 * c >= thr ? 6 : 32 * c >= thr ? 7 : 8;
 }
 
+template <int L>
 __global__ void sym_plan_kernel(const int* __restrict__ cs, ChainDimsP cd, int nsub, float re2, float margin,
                                 u32* __restrict__ masks, uint4* __restrict__ stage, u32 cap,
                                 u32* __restrict__ counter, const int* __restrict__ stop) {
+  constexpr int MW = sym_mark_words(L) + 1;
   if (*stop) return;
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a > nsub) return;
-  u32 w[SYM_MASK_WORDS];
+  u32 w[MW];
 #pragma unroll
-  for (int i = 0; i < SYM_MASK_WORDS; ++i) w[i] = 0u;
+  for (int i = 0; i < MW; ++i) w[i] = 0u;
   const int pa = a < nsub ? cs[a + 1] - cs[a] : 0;
   if (pa >= SYM_MIN_SMALL) {
     const unsigned long long thr = __ldcg(reinterpret_cast<const unsigned long long*>(counter + 6));
-    const int cell = a / SYM_LOCAL, ca = a % SYM_LOCAL;
+    const int cell = a / L, ca = a % L;
     const int gx = cell % cd.Mx, gy = (cell / cd.Mx) % cd.My, gz = cell / (cd.Mx * cd.My);
     u32 dead = 0u;
     for (int k = 0; k < NNB; ++k) {
@@ -607,8 +610,8 @@ __global__ void sym_plan_kernel(const int* __restrict__ cs, ChainDimsP cd, int n
       const int nb = nx + ny * cd.Mx + nz * cd.Mx * cd.My;
       bool alive = false;  // something one-sided left toward this neighbour cell
 #pragma unroll
-      for (int cb = 0; cb < SYM_LOCAL; ++cb) {
-        const int b = nb * SYM_LOCAL + cb;
+      for (int cb = 0; cb < L; ++cb) {
+        const int b = nb * L + cb;
         if (b == a) {
           alive = true;
           continue;
@@ -620,9 +623,9 @@ __global__ void sym_plan_kernel(const int* __restrict__ cs, ChainDimsP cd, int n
           alive = true;
           continue;
         }
-        const int sb = k * SYM_LOCAL + cb;
+        const int sb = k * L + cb;
 #pragma unroll
-        for (int i = 0; i < SYM_MASK_WORDS; ++i)
+        for (int i = 0; i < MW - 1; ++i)
           if ((sb >> 5) == i) w[i] |= 1u << (sb & 31);
         if (k > 13 || (k == 13 && cb > ca)) {
           const int bk = sym_bucket(cost, thr);
@@ -634,10 +637,10 @@ __global__ void sym_plan_kernel(const int* __restrict__ cs, ChainDimsP cd, int n
       }
       if (!alive) dead |= 1u << k;
     }
-    w[SYM_MARK_WORDS] = dead;
+    w[MW - 1] = dead;
   }
 #pragma unroll
-  for (int i = 0; i < SYM_MASK_WORDS; ++i) masks[(size_t)a * SYM_MASK_WORDS + i] = w[i];
+  for (int i = 0; i < MW; ++i) masks[(size_t)a * MW + i] = w[i];
 }
 
 // subcol[i] = the sub-column (or the outside bucket) of sorted particle i.
@@ -790,12 +793,13 @@ __device__ __forceinline__ void sym_unit(const SlotCtx& c, float4* __restrict__ 
                                          float4 (*jbuf)[32], float4* part, u32 tab_base, int lane, int warp) {
   const ChainDimsP& cd = c.cd;
   const int p = (int)unit.x, q = (int)unit.y;
-  const int cp = p / SYM_LOCAL, ca = p % SYM_LOCAL, cq = q / SYM_LOCAL, cb = q % SYM_LOCAL;
+  const int L = cd.sub * cd.sub;
+  const int cp = p / L, ca = p % L, cq = q / L, cb = q % L;
   const int gx = cp % cd.Mx, gy = (cp / cd.Mx) % cd.My, gz = cp / (cd.Mx * cd.My);
   const int nx = cq % cd.Mx, ny = (cq / cd.Mx) % cd.My, nz = cq / (cd.Mx * cd.My);
   const int k = (nx - gx + 1) + 3 * (ny - gy + 1) + 9 * (nz - gz + 1);
-  float4* __restrict__ si = sym_slots + (size_t)(k * SYM_LOCAL + cb) * c.n;
-  float4* __restrict__ sj = sym_slots + (size_t)((NNB - 1 - k) * SYM_LOCAL + ca) * c.n;
+  float4* __restrict__ si = sym_slots + (size_t)(k * L + cb) * c.n;
+  float4* __restrict__ sj = sym_slots + (size_t)((NNB - 1 - k) * L + ca) * c.n;
   const float h0 = sqrtf(c.re2 - sym_gap2(cd, gx, gz, ca, nx, nz, cb, c.gap_margin));
   const int bb = c.cell_start[q], be = c.cell_start[q + 1];
   if (COOP) {
@@ -932,7 +936,7 @@ __global__ void __maxnreg__(128) pair_slot_kernel(
     const float4* __restrict__ pm, int n, const int* __restrict__ cell_start,
     const int2* __restrict__ items, const u32* __restrict__ nitems_p, const u32* __restrict__ heavy,
     u32 heavy_cap, u32* __restrict__ counter, ChainDimsP cd, PairParams pp, const float* __restrict__ table,
-    float4* __restrict__ slots, u32 unit_stride, const u32* __restrict__ sym_masks, u32 sym_cap,
+    float4* __restrict__ slots, u32 unit_stride, const u32* __restrict__ sym_masks, int sym_words, u32 sym_cap,
     float4* __restrict__ sym_slots, const uint2* __restrict__ sym_units, const int* __restrict__ stop) {
   static_assert(SLOT_PART >= SLOT_SLICE && SLOT_PART >= SYM_SLICE, "partial-sum buffer too small");
   if (*stop) return;
@@ -952,7 +956,7 @@ __global__ void __maxnreg__(128) pair_slot_kernel(
   // least the cutoff (with a margin far above the rounding of the sub-column assignment)
   const bool sym_on = EQM && sym_masks && __ldcg(&counter[SLOT_SYM_TOTAL]) <= sym_cap;
   const SlotCtx c{pm, cell_start, items, slots, n, cd, pp.re2, sc, 1e-3f * fminf(cd.HCsx, cd.HCsz), pp.ysort, cn,
-                  sym_on ? sym_masks : nullptr};
+                  sym_on ? sym_masks : nullptr, sym_words};
   const u32 nall = *nitems_p * NNB;  // every slice once per neighbour cell
   const u32 nh = __ldcg(&counter[2]), nm = __ldcg(&counter[3]);
   const bool listed = (unsigned long long)nh + nm <= heavy_cap;  // both lists complete
@@ -1017,7 +1021,7 @@ __global__ void __maxnreg__(128) pair_slot_kernel(
     const u32 it = base + lane;
     bool live = lane < SLOT_REST_BATCH && it < nall && (it / NNB) % unit_stride == 0;  // sampled: every stride-th slice
     if (live && listed) live = slot_cost(cell_start, cd, items[it / NNB], (int)(it % NNB)) < thr / 4;
-    if (live && c.sym_masks) live = !sym_dead(c.sym_masks, items[it / NNB].x, (int)(it % NNB));
+    if (live && c.sym_masks) live = !sym_dead(c.sym_masks, c.sym_words, items[it / NNB].x, (int)(it % NNB));
     for (u32 m = __ballot_sync(0xFFFFFFFFu, live); m; m &= m - 1)
       slot_unit<EQM, EXACT, false>(c, base + (u32)(__ffs(m) - 1), jbuf, part, tab_base, lane, warp);
   }
@@ -1026,7 +1030,9 @@ __global__ void __maxnreg__(128) pair_slot_kernel(
 // Sum of the 27 slots in slot order (Kahan), each direction's one-sided slot followed by its
 // symmetric slots in sub-column order (when the pass had a symmetric part: sym_slots non-null and
 // the unit list complete), plus the PM acceleration; in a run the kick, the drift, the unit round
-// trip and the escape test, writing the new state to the other buffers.
+// trip and the escape test, writing the new state to the other buffers.  L: the symmetric
+// part's sub-columns per cell.
+template <int L>
 __global__ void __launch_bounds__(256) pair_epilogue_kernel(
     const float4* __restrict__ pm, const float4* __restrict__ vi, const float4* __restrict__ acc_pm,
     const float4* __restrict__ slots, int n, StepParams sp, float kick, int drift, int kdk,
@@ -1038,17 +1044,18 @@ __global__ void __launch_bounds__(256) pair_epilogue_kernel(
   if (i >= n) return;
   float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
   if (sym_slots && __ldcg(&counter[SLOT_SYM_TOTAL]) <= sym_cap) {
-    const u32* mw = sym_masks + (size_t)subcol[i] * SYM_MASK_WORDS;
-    u32 w[SYM_MASK_WORDS];
+    constexpr int MW = sym_mark_words(L) + 1;
+    const u32* mw = sym_masks + (size_t)subcol[i] * MW;
+    u32 w[MW];
 #pragma unroll
-    for (int t = 0; t < SYM_MASK_WORDS; ++t) w[t] = mw[t];
+    for (int t = 0; t < MW; ++t) w[t] = mw[t];
 #pragma unroll
     for (int k = 0; k < NNB; ++k) {
-      // bits 9k .. 9k + 8 (constants once k is unrolled); a dead direction has no one-sided
-      // slot (its units were skipped)
-      u32 field = sym_field(w, k);
-      const int lo = k * SYM_LOCAL;
-      if (!((w[SYM_MARK_WORDS] >> k) & 1u)) {
+      // bits k L .. k L + L - 1 (constants once k is unrolled); a dead direction has no
+      // one-sided slot (its units were skipped)
+      u32 field = sym_field<L>(w, k);
+      const int lo = k * L;
+      if (!((w[MW - 1] >> k) & 1u)) {
         const float4 v = slots[(size_t)k * n + i];
         kahan_add(sx, cx, v.x);
         kahan_add(sy, cy, v.y);
@@ -1186,12 +1193,14 @@ int slot_heavy_capacity(int nitems_max) {
   return (int)(units < (1 << 22) ? units : (1 << 22));
 }
 
-int sym_mask_words() { return SYM_MASK_WORDS; }
+bool sym_supported(int sub) { return sub >= 3 && sub <= 5; }
 
-// Units a symmetric pass can list: up to 13 x 9 upper-half neighbours and 8 within the cell per
-// sub-column of at least SYM_MIN_SMALL particles, at most 2^24.
-int sym_unit_capacity(int nsub, int n) {
-  constexpr long long per_sub = 13LL * SYM_LOCAL + SYM_LOCAL - 1;
+int sym_mask_words(int sub) { return sym_mark_words(sub * sub) + 1; }
+
+// Units a symmetric pass can list: up to 13 L upper-half neighbours and L - 1 within the cell per
+// sub-column of at least SYM_MIN_SMALL particles (L = sub^2 sub-columns per cell), at most 2^24.
+int sym_unit_capacity(int nsub, int n, int sub) {
+  const long long per_sub = 13LL * sub * sub + sub * sub - 1;
   const long long units = per_sub * (long long)std::max(std::min(nsub, n / SYM_MIN_SMALL), 1);
   return (int)(units < (1 << 24) ? units : (1 << 24));
 }
@@ -1212,8 +1221,9 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
   const bool exact = !pp.use_table && pp.eps2 == 0.f;
   const bool slotted = (pp.use_table || exact) && !npairs && slots;
   const int slice = slotted ? SLOT_SLICE : 32;
-  // the symmetric part: equal masses, 3 x 3 y-sorted sub-columns, every slice (not sampled)
-  const bool sym_on = slotted && sym && sym->enabled && sym->slots && equal_mass && chd.sub == 3 &&
+  // the symmetric part: equal masses, 3 x 3 to 5 x 5 y-sorted sub-columns, every slice (not
+  // sampled)
+  const bool sym_on = slotted && sym && sym->enabled && sym->slots && equal_mass && sym_supported(chd.sub) &&
                       pp.ysort && ustride == 1 && nitems_max > 0 && n > 0;
   item_count_kernel<<<(ntot + 255) / 256, 256, 0, st>>>(cell_start, ntot, item_cnt, slice, stop);
   int rc = exclusive_scan(item_cnt, item_off, ntot, nitems, scan_tmp, st);
@@ -1230,12 +1240,12 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
                                           (unsigned long long)num_sms * SLOT_CTAS_PER_SM * SLOT_WARPS, ustride,
                                           stop);
     if (sym_on) {
-      const int nsub = ncells * SYM_LOCAL;
+      const int nsub = ncells * chd.sub * chd.sub;
       // units buffer: 2 cap uint2 of staging (as cap uint4), then the laid-out list
       uint4* stage = reinterpret_cast<uint4*>(sym->units);
-      sym_plan_kernel<<<(nsub + 1 + 255) / 256, 256, 0, st>>>(cell_start, cd, nsub, pp.re2,
-                                                             1e-3f * fminf(cd.HCsx, cd.HCsz), sym->masks,
-                                                             stage, sym->cap, counter, stop);
+      auto plan = chd.sub == 5 ? sym_plan_kernel<25> : chd.sub == 4 ? sym_plan_kernel<16> : sym_plan_kernel<9>;
+      plan<<<(nsub + 1 + 255) / 256, 256, 0, st>>>(cell_start, cd, nsub, pp.re2, 1e-3f * fminf(cd.HCsx, cd.HCsz),
+                                                  sym->masks, stage, sym->cap, counter, stop);
       sym_scatter_kernel<<<num_sms * 4, 256, 0, st>>>(stage, sym->units + 2 * (size_t)sym->cap, sym->cap, counter,
                                                        stop);
       subcol_kernel<<<pb, 256, 0, st>>>(cell_start, items, nitems, sym->subcol, stop);
@@ -1259,10 +1269,13 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
                            : (exact ? pair_slot_kernel<false, true> : pair_slot_kernel<false, false>);
     kern<<<num_sms * SLOT_CTAS_PER_SM, SLOT_THREADS, SLOT_SMEM, st>>>(
         pm, n, cell_start, items, nitems, heavy, heavy_cap, counter, cd, pp, table, slots, ustride,
-        sym_on ? sym->masks : nullptr, sym_on ? sym->cap : 0u, sym_on ? sym->slots : nullptr,
-        sym_on ? sym->units + 2 * (size_t)sym->cap : nullptr, stop);
+        sym_on ? sym->masks : nullptr, sym_mask_words(chd.sub), sym_on ? sym->cap : 0u,
+        sym_on ? sym->slots : nullptr, sym_on ? sym->units + 2 * (size_t)sym->cap : nullptr, stop);
+    auto epilogue = !sym_on || chd.sub == 3 ? pair_epilogue_kernel<9>
+                    : chd.sub == 4          ? pair_epilogue_kernel<16>
+                                            : pair_epilogue_kernel<25>;
     if (n > 0)
-      pair_epilogue_kernel<<<(n + 255) / 256, 256, 0, st>>>(
+      epilogue<<<(n + 255) / 256, 256, 0, st>>>(
           pm, vi, acc_pm, slots, n, sp, kick, drift, kdk, pm_out, vi_out, acc_out,
           sym_on ? sym->slots : nullptr, sym_on ? sym->masks : nullptr, sym_on ? sym->subcol : nullptr, counter,
           sym_on ? sym->cap : 0u, stop);

@@ -501,6 +501,12 @@ class P3MMethod:
         check(lib().pmgb_p3m_get_symmetric(self._h, C.byref(e), C.byref(u)))
         return bool(e.value), int(u.value)
 
+    def subColumns(self) -> int:
+        """Sub-columns per cell axis of the pair pass (1, or 3 to 5; fixed at creation)."""
+        s = C.c_int(0)
+        check(lib().pmgb_p3m_get_subcolumns(self._h, C.byref(s)))
+        return int(s.value)
+
     def pairCount(self) -> int:
         """Ordered pairs within the cutoff in the last force evaluation."""
         c = C.c_ulonglong(0)

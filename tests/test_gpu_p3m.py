@@ -202,17 +202,20 @@ def _sym_case(n, table, seed, grid=64, spread=(0.6, 2.5)):
     return cfg, q, pos, vel, mass
 
 
-@pytest.mark.parametrize("table", [1, 0])
-def test_symmetric_pass_matches_one_sided(gpu_lib, table):
+@pytest.mark.parametrize("table,n,grid,sub", [(1, 20000, 64, 3), (0, 20000, 64, 3), (1, 40000, 64, 4),
+                                              (0, 40000, 64, 4), (1, 60000, 64, 5), (0, 60000, 32, 5)])
+def test_symmetric_pass_matches_one_sided(gpu_lib, table, n, grid, sub):
     """The pair pass's symmetric part (light sub-column pairs evaluated once, each side into a
     slot of its own, summed in a fixed order): it takes a large share of the pairs here, its
     forces equal the one-sided pass's to float rounding and the FP64 oracle's within the parity
-    bar, and two evaluations are bit-identical (every slot has one writer)."""
+    bar, and two evaluations are bit-identical (every slot has one writer).  With 3 x 3, 4 x 4
+    and 5 x 5 sub-columns per cell (10^3 cells of 20, 40 or 60 particles on average, 5^3 of 480)."""
     from conftest import err_stats
-    cfg, q, pos, vel, mass = _sym_case(60000, table, seed=21)
+    cfg, q, pos, vel, mass = _sym_case(n, table, seed=21, grid=grid)
     pm, p3m = make_p3m(cfg, q, pos, vel, mass)
     on, _ = p3m.symmetric()
     assert on
+    assert p3m.subColumns() == sub
     p3m.force()
     acc_sym = pm.getParticles()[2].copy()
     units = p3m.symmetric()[1]
@@ -240,6 +243,32 @@ def test_symmetric_pass_matches_one_sided(gpu_lib, table):
     pm.close()
 
 
+@pytest.mark.parametrize("grid,n,ysort,sub", [(64, 20000, 1, 3), (64, 40000, 1, 4), (32, 30000, 1, 5),
+                                              (32, 30000, 0, 1)])
+def test_subcolumns_per_cell_and_cell_lists(gpu_lib, grid, n, ysort, sub):
+    """Sub-columns per cell axis: 5 where the particles average at least 48 per chaining-mesh cell,
+    4 from 32, else 3, 1 for the reference's unsorted lists; the cell lists handed out are the
+    reference's whole-cell lists either way (vs the oracle's ChainingMesh fill, bit for bit)."""
+    cfg, q, pos, vel, mass = _sym_case(n, 1, seed=31, grid=grid)
+    q = O.P3MConfig(comp_box=q.comp_box, cutoff=q.cutoff, diameter=q.diameter, softening=0.0,
+                    cloud_shape=1, use_table=1, y_sorting=ysort)
+    pm, p3m = make_p3m(cfg, q, pos, vel, mass)
+    assert p3m.subColumns() == sub
+    pc = (pos / np.float32(cfg.H)).astype(np.float32)
+    pm.setParticles(pc, np.zeros_like(pc), units="code")  # the same code-unit positions as the oracle's
+    p3m.force()
+    order, counts, dims = p3m.getCellLists()
+    o_ref, c_ref, d_ref = O.port_chaining_mesh(q, cfg.H, pc, ysort)
+    assert dims == d_ref
+    if ysort:
+        nc = int(np.prod(dims))
+        assert sub == (5 if n >= 48 * nc else 4 if n >= 32 * nc else 3)
+    np.testing.assert_array_equal(counts, c_ref)
+    np.testing.assert_array_equal(order, o_ref)
+    p3m.close()
+    pm.close()
+
+
 def test_symmetric_pass_run_bit_identical(gpu_lib):
     """A multi-step P3M run with the symmetric part on: repeated runs from the same state give
     bit-identical particles, and the end state stays within float rounding of the one-sided
@@ -259,7 +288,7 @@ def test_symmetric_pass_run_bit_identical(gpu_lib):
 
 
 def test_symmetric_pass_only_where_it_applies(gpu_lib):
-    """The symmetric part needs equal masses and y-sorted 3 x 3 sub-columns: with unequal masses
+    """The symmetric part needs equal masses and y-sorted sub-columns: with unequal masses
     the pass lists no symmetric unit (and still matches the FP64 oracle), with unsorted cell
     lists the handle has no symmetric slots at all."""
     cfg, q, pos, vel, mass = _sym_case(20000, 1, seed=27, grid=32)
