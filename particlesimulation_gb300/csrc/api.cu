@@ -739,7 +739,12 @@ int p3m_create_internal(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out,
   // the symmetric part of the pair pass (y-sorted lists): 27 sub^2 slots per particle (3.9, 6.9
   // or 10.8 KB), the mask words per sub-column, the unit list; left off if it would take more
   // than a quarter of the free device memory or the allocation fails
-  if (sym_supported(q->cd.sub) && pm->n > 0) {
+  bool pads_vanish = true;  // exact mode: the symmetric part's padded candidates add exactly 0
+  if (!cfg->use_table && cfg->softening == 0.f && (rc = exact_mode_pads_vanish(pm->st, &pads_vanish))) {
+    pmgb_p3m_destroy(q);
+    return rc;
+  }
+  if (sym_supported(q->cd.sub) && pm->n > 0 && pads_vanish) {
     const size_t n = (size_t)pm->n, nslot = 27 * (size_t)q->cd.sub * q->cd.sub;
     q->sym.cap = (u32)sym_unit_capacity(q->nsub, pm->n, q->cd.sub);
     void* ptr[4] = {nullptr, nullptr, nullptr, nullptr};

@@ -63,6 +63,7 @@ int sym_unit_capacity(int nsub, int n, int sub);
 constexpr int kSlotSymTotalWord = 28;  // counter word of the symmetric units a pass listed
 int sym_mask_words(int sub);  // mask words per sub-column with sub x sub sub-columns per cell
 bool sym_supported(int sub);  // sub-column counts the symmetric part is built for
+int exact_mode_pads_vanish(cudaStream_t st, bool* vanish);  // the symmetric part's exact-mode condition
 
 int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const int* cell_start,
                 const ChainDims& cd, u32* item_cnt, u32* item_off, u32* scan_tmp, u32* nitems, int2* items,

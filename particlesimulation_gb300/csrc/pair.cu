@@ -366,6 +366,14 @@ __device__ __forceinline__ unsigned long long slot_cost(const int* __restrict__ 
          (unsigned long long)(__ldg(&cell_start[(nb + 1) * sub2]) - __ldg(&cell_start[nb * sub2]));
 }
 
+// rsqrt.approx of 1 and its cube as the exact-mode pass computes them (rsqrt_approx, then two
+// multiplies).
+__global__ void rsqrt_one_kernel(float* out) {
+  const float r1 = rsqrt_approx(1.0f);
+  out[0] = r1;
+  out[1] = r1 * r1 * r1;
+}
+
 // Per-launch constants of the table pass.
 struct SlotCtx {
   const float4* __restrict__ pm;
@@ -467,10 +475,12 @@ __device__ __forceinline__ void slot_unit(const SlotCtx& c, u32 it, float4 (*jbu
         const int cnt = min(32, e - j0);
 #pragma unroll
         for (int u = 0; u < SLOT_IPL; ++u) I[u].px = I[u].py = I[u].pz = 0.f;
-        // unrolled 16 deep (32 independent pair chains per lane in flight; two bodies cover a full
-        // chunk): on the 262,144-particle disk 6.23 ms at 8, 6.17 at 16, 6.29 at 32 and 6.8 at
-        // 24 (remainder iterations)
-#pragma unroll 16
+        // unrolled 4 deep: the kernel also holds the symmetric units' code, and shorter loop
+        // bodies keep the instruction cache warm (1,048,576-particle disk, reduced / full
+        // cutoff: 28.0 / 76.7 ms at 16, 27.8 / 75.6 at 8, 27.3 / 75.3 at 4, 27.7 / 75.7 at 2;
+        // 262,144-particle disk 5.97 / 5.92 / 5.97 / 6.06 ms; 4 deep already with the tail
+        // group of the symmetric windows run as a full group)
+#pragma unroll 4
         for (int s = 0; s < cnt; ++s) {
           const float4 q = jbuf[warp][s];
 #pragma unroll
@@ -679,7 +689,7 @@ __global__ void sym_scatter_kernel(const uint4* __restrict__ stage, uint2* __res
 // One candidate q against the lane's SYM_IPL i particles: their sums accumulate as in slot_pair;
 // v = the sum of the pair forces f d, the candidate's share of its j side (negated later).
 // MASKED: each force is multiplied by w[u] (0 for lanes past a slice's end, which hold copies
-// of its last particle, and for candidates past a chunk's end: neither may reach a sum).
+// of its last particle and may not reach a sum).
 template <bool EXACT, bool MASKED>
 __device__ __forceinline__ void sym_pair(SymI (&I)[SYM_IPL], const float4& q, u32 tab_base, float cn,
                                          const float (&w)[SYM_IPL], float (&v)[3]) {
@@ -738,23 +748,17 @@ __device__ __forceinline__ void sym_window(const SlotCtx& c, SymI (&I)[SYM_IPL],
 #pragma unroll
     for (int u = 0; u < SYM_IPL; ++u) I[u].px = I[u].py = I[u].pz = 0.f;
     float tx = 0.f, ty = 0.f, tz = 0.f;
+    // a partial last group runs as a full one: the staged entries past the window are far-away
+    // points (3e30), whose |r|^2 saturates to the table's last segment, where the force is
+    // exactly 0 (the table: segments 499.. are zero; exact mode: the Newton term and segment
+    // 499's constant cancel exactly, which the handle checks before it enables this part), so
+    // they add nothing to the i sides, and their j sides are never stored
 #pragma unroll 1
     for (int g = 0; 4 * g < cnt; ++g) {
       float v[4][3];
-      if (4 * g + 4 <= cnt) {
 #pragma unroll
-        for (int m = 0; m < 4; ++m)
-          sym_pair<EXACT, MASKED>(I, jbuf[warp][4 * g + (m ^ swz)], tab_base, c.cn, w, v[m]);
-      } else {
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          const float cw = 4 * g + (m ^ swz) < cnt ? 1.f : 0.f;
-          float wm[SYM_IPL];
-#pragma unroll
-          for (int u = 0; u < SYM_IPL; ++u) wm[u] = MASKED ? w[u] * cw : cw;
-          sym_pair<EXACT, true>(I, jbuf[warp][4 * g + (m ^ swz)], tab_base, c.cn, wm, v[m]);
-        }
-      }
+      for (int m = 0; m < 4; ++m)
+        sym_pair<EXACT, MASKED>(I, jbuf[warp][4 * g + (m ^ swz)], tab_base, c.cn, w, v[m]);
       // lanes l and l ^ 16 hold each other's slots 2, 3 in their slots 0, 1 (swz differs in bit
       // 1), lanes l and l ^ 8 each other's slot 1 in their slot 0 (bit 0); then bits 2..0
       float x[3];
@@ -1194,6 +1198,29 @@ int slot_heavy_capacity(int nitems_max) {
 }
 
 bool sym_supported(int sub) { return sub >= 3 && sub <= 5; }
+
+// The symmetric part's padded candidates (sym_window) add exactly nothing in exact mode only if
+// the Newton term at |r| = re, cn r1^3, is exactly the value segment 499 cancels, which holds
+// when rsqrt.approx(1) and its cube are exactly 1 (GB300: they are).  Checked once per process.
+int exact_mode_pads_vanish(cudaStream_t st, bool* vanish) {
+  static int known = -1;
+  if (known < 0) {
+    float* d = nullptr;
+    float h[2] = {0.f, 0.f};
+    PMGB_CUDA_TRY(cudaMalloc(&d, 2 * sizeof(float)));
+    rsqrt_one_kernel<<<1, 1, 0, st>>>(d);
+    const cudaError_t e1 = cudaGetLastError();
+    const cudaError_t e2 = cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, st);
+    const cudaError_t e3 = cudaStreamSynchronize(st);
+    cudaFree(d);
+    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess)
+      return set_error("rsqrt probe failed"), PMGB_ECUDA;
+    count_launches(1);
+    known = h[0] == 1.0f && h[1] == 1.0f ? 1 : 0;
+  }
+  *vanish = known == 1;
+  return PMGB_OK;
+}
 
 int sym_mask_words(int sub) { return sym_mark_words(sub * sub) + 1; }
 
