@@ -989,45 +989,59 @@ __global__ void __maxnreg__(128) pair_slot_kernel(
       }
     }
   }
-  // warps: the two longest buckets of symmetric units, the medium one-sided units, the rest of
-  // the symmetric units
-  auto warp_sym = [&](int b0, int b1) {
-    if constexpr (EQM) {
-      if (!sym_on) return;
-      for (int b = b0; b < b1; ++b) {
-        const u32 cnt = __ldcg(&counter[SLOT_SYM_COUNT + b]), off = sym_bucket_start(counter, b);
-        for (;;) {
-          u32 m = 0;
-          if (lane == 0) m = atomicAdd(&counter[SLOT_SYM_TAKEN + b], 1u);
-          m = __shfl_sync(0xFFFFFFFFu, m, 0);
-          if (m >= cnt) break;
-          sym_unit<EXACT, false>(c, sym_slots, __ldg(&sym_units[off + m]), jbuf, part, tab_base, lane, warp);
-        }
+  // warps: one loop with one call site per kind of unit, so that each unit's code is in the
+  // kernel once (the instruction cache holds less).  Phases: 0 the two longest buckets of
+  // symmetric units, 1 the medium one-sided units, 2 the other symmetric buckets, 3 the rest of
+  // the one-sided units, SLOT_REST_BATCH per fetch (each lane tests one: sampled slice, not
+  // listed, not a dead direction of the symmetric part), the live ones in unit order.
+  const bool wsym = EQM && sym_on;
+  int ph = wsym ? 0 : 1, b = SYM_NB_CTA;
+  u32 live_m = 0u, base = 0u;
+#pragma unroll 1
+  for (;;) {
+    if (ph == 0 || ph == 2) {
+      if (b == (ph == 0 ? SYM_NB_CTA + 2 : SYM_NB)) {
+        ++ph;
+        continue;
       }
+      u32 m = 0;
+      if (lane == 0) m = atomicAdd(&counter[SLOT_SYM_TAKEN + b], 1u);
+      m = __shfl_sync(0xFFFFFFFFu, m, 0);
+      if (m >= __ldcg(&counter[SLOT_SYM_COUNT + b])) {
+        ++b;
+        continue;
+      }
+      if constexpr (EQM)
+        sym_unit<EXACT, false>(c, sym_slots, __ldg(&sym_units[sym_bucket_start(counter, b) + m]), jbuf, part,
+                               tab_base, lane, warp);
+      continue;
     }
-  };
-  warp_sym(SYM_NB_CTA, SYM_NB_CTA + 2);
-  for (;;) {
-    u32 m = 0;
-    if (lane == 0) m = atomicAdd(&counter[1], 1u);
-    m = __shfl_sync(0xFFFFFFFFu, m, 0);
-    if (m >= nmedium) break;
-    slot_unit<EQM, EXACT, false>(c, __ldg(&heavy[heavy_cap - 1 - m]), jbuf, part, tab_base, lane, warp);
-  }
-  warp_sym(SYM_NB_CTA + 2, SYM_NB);
-  // the rest, SLOT_REST_BATCH units per fetch: each lane tests one (sampled slice, not listed,
-  // not a dead direction of the symmetric part) and the warp runs the live ones in unit order
-  for (;;) {
-    u32 base = 0;
-    if (lane == 0) base = atomicAdd(&counter[8], (u32)SLOT_REST_BATCH);
-    base = __shfl_sync(0xFFFFFFFFu, base, 0);
-    if (base >= nall) break;
-    const u32 it = base + lane;
-    bool live = lane < SLOT_REST_BATCH && it < nall && (it / NNB) % unit_stride == 0;  // sampled: every stride-th slice
-    if (live && listed) live = slot_cost(cell_start, cd, items[it / NNB], (int)(it % NNB)) < thr / 4;
-    if (live && c.sym_masks) live = !sym_dead(c.sym_masks, c.sym_words, items[it / NNB].x, (int)(it % NNB));
-    for (u32 m = __ballot_sync(0xFFFFFFFFu, live); m; m &= m - 1)
-      slot_unit<EQM, EXACT, false>(c, base + (u32)(__ffs(m) - 1), jbuf, part, tab_base, lane, warp);
+    u32 unit;
+    if (ph == 1) {
+      u32 m = 0;
+      if (lane == 0) m = atomicAdd(&counter[1], 1u);
+      m = __shfl_sync(0xFFFFFFFFu, m, 0);
+      if (m >= nmedium) {
+        ph = wsym ? 2 : 3;
+        continue;
+      }
+      unit = __ldg(&heavy[heavy_cap - 1 - m]);
+    } else {
+      if (!live_m) {
+        if (lane == 0) base = atomicAdd(&counter[8], (u32)SLOT_REST_BATCH);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= nall) break;
+        const u32 it = base + lane;
+        bool live = lane < SLOT_REST_BATCH && it < nall && (it / NNB) % unit_stride == 0;  // sampled: every stride-th slice
+        if (live && listed) live = slot_cost(cell_start, cd, items[it / NNB], (int)(it % NNB)) < thr / 4;
+        if (live && c.sym_masks) live = !sym_dead(c.sym_masks, c.sym_words, items[it / NNB].x, (int)(it % NNB));
+        live_m = __ballot_sync(0xFFFFFFFFu, live);
+        if (!live_m) continue;
+      }
+      unit = base + (u32)(__ffs(live_m) - 1);
+      live_m &= live_m - 1;
+    }
+    slot_unit<EQM, EXACT, false>(c, unit, jbuf, part, tab_base, lane, warp);
   }
 }
 
