@@ -553,7 +553,7 @@ def closure_headline(args, w, flush_l2, clocks, rank, world):
     q = w.p3m
 
     def judged_step(s):
-        iv = 1 if s % JUDGE_INTERVAL == 0 else 0  # judge before this step (learned mode only)
+        iv = 1 if s % JUDGE_INTERVAL == 0 else 0  # judge this step after it ran (learned mode only)
         esc, _, fb, _ = cl.run(1, args.closure_bound, iv, JUDGE_STRIDE)
         if esc:
             raise RuntimeError("a particle left the box")

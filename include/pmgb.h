@@ -373,9 +373,13 @@ int pmgb_closure_set_params(pmgb_closure* c, const float* params, int count);
  * particle by index (full pass).  The learned force is the last step's when that step was
  * learned and the particles have not moved since. */
 int pmgb_closure_judge(pmgb_closure* c, int stride, float* median_rel_err);
-/* n_steps run-loop iterations in the current mode; in PMGB_CLOSURE_LEARNED the judge runs every
- * judge_interval steps and a median error above `bound` switches the rest of the run to plain
- * P3M (*fallback_step = that step, else -1). */
+/* n_steps run-loop iterations in the current mode.  In PMGB_CLOSURE_LEARNED every
+ * judge_interval-th step (0, judge_interval, ...) is judged after it ran, at the positions it
+ * drifted to (pmgb_closure_judge on the learned force it used); a median error above `bound` has
+ * the step taken again from its start with plain P3M, and the rest of the run too
+ * (*fallback_step = that step, else -1), so no step keeps a rejected force.  The step's start
+ * state is kept in 32 bytes per particle of device memory, allocated on the first judged run.
+ * device_ms counts both attempts of a rejected step. */
 int pmgb_closure_run(pmgb_closure* c, int n_steps, float bound, int judge_interval,
                      int judge_stride, int* steps_done, int* fallback_step, float* device_ms);
 /* Test support: the 67 inputs of every particle (original order) and its patch mass; the

@@ -903,6 +903,9 @@ struct pmgb_closure {
   float* accF = nullptr;        // scratch: 3n floats each
   float* accR = nullptr;
   unsigned char* judged = nullptr;  // n flags: particles a sampled judge pass covered
+  float4* save_pm = nullptr;    // a judged step's start state (n each), to take it again
+  float4* save_vi = nullptr;
+  unsigned char* save_diag = nullptr;  // and its diagnostics' running state (32 bytes)
   int adam_t = 0;
   unsigned long long seed = 0;
 };
@@ -1052,7 +1055,8 @@ int pmgb_closure_destroy(pmgb_closure* c) {
   if (c->full) pmgb_p3m_destroy(c->full);
   if (c->reduced) pmgb_p3m_destroy(c->reduced);
   void* ptrs[] = {c->occ_fx, c->occ, c->params, c->adam_m, c->adam_v, c->grad, c->gw, c->lossw,
-                  c->loss, c->img, c->X, c->T, c->accF, c->accR, c->judged};
+                  c->loss, c->img, c->X, c->T, c->accF, c->accR, c->judged, c->save_pm, c->save_vi,
+                  c->save_diag};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete c;
@@ -1230,40 +1234,71 @@ int pmgb_closure_judge(pmgb_closure* c, int stride, float* median_rel_err) {
   return PMGB_OK;
 }
 
-// Runs n_steps loop iterations (pmgb_pm_advance) in the learned mode with the judge every
-// judge_interval steps (0 = never): if its median relative error exceeds `bound`, the rest of
-// the run uses plain full-cutoff P3M (*fallback_step = the step, else -1).
+// Runs n_steps loop iterations (pmgb_pm_advance, one at a time).  In the learned mode every
+// judge_interval-th step (s = 0, judge_interval, ...) is judged after it ran: the learned force it
+// used, at the positions it drifted to, against plain P3M there (pmgb_closure_judge).  If the
+// median relative difference exceeds `bound`, the step is taken again from its saved start state
+// (positions, velocities, particle order, diagnostics' running state) with plain full-cutoff P3M,
+// and so is the rest of the run (*fallback_step = the step, else -1): no step keeps a force the
+// judge rejected.  device_ms counts both attempts of a rejected step.
 int pmgb_closure_run(pmgb_closure* c, int n_steps, float bound, int judge_interval,
                      int judge_stride, int* steps_done, int* fallback_step, float* device_ms) {
   if (!c) return set_error("null handle"), PMGB_EINVAL;
   if (fallback_step) *fallback_step = -1;
+  pmgb_pm* h = c->pm;
+  const size_t n = (size_t)h->n;
+  if (c->mode == PMGB_CLOSURE_LEARNED && judge_interval > 0 && !c->save_pm) {
+    if (cudaMalloc(&c->save_pm, std::max(n, (size_t)1) * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc(&c->save_vi, std::max(n, (size_t)1) * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc(&c->save_diag, 32) != cudaSuccess) {
+      cudaGetLastError();
+      return set_error("cudaMalloc failed (closure step state)"), PMGB_ENOMEM;
+    }
+  }
   float total_ms = 0.f;
   int done = 0;
+  auto finish = [&](int rc) {
+    if (steps_done) *steps_done = done;
+    if (device_ms) *device_ms = total_ms;
+    return rc;
+  };
   for (int s = 0; s < n_steps; ++s) {
-    if (c->mode == PMGB_CLOSURE_LEARNED && judge_interval > 0 && s % judge_interval == 0) {
-      float err = 0.f;
-      int rc = pmgb_closure_judge(c, judge_stride, &err);
+    const bool judge = c->mode == PMGB_CLOSURE_LEARNED && judge_interval > 0 && s % judge_interval == 0;
+    const int cur0 = h->cur, since0 = h->since_sort;
+    if (judge) {
+      PMGB_CUDA_TRY(cudaMemcpyAsync(c->save_pm, h->pm[cur0], n * sizeof(float4), cudaMemcpyDeviceToDevice, h->st));
+      PMGB_CUDA_TRY(cudaMemcpyAsync(c->save_vi, h->vi[cur0], n * sizeof(float4), cudaMemcpyDeviceToDevice, h->st));
+      int rc = diag_save(h, c->save_diag);
       if (rc) return rc;
-      if (err > bound) {
-        set_mode(c, PMGB_CLOSURE_FULL);
-        if (fallback_step) *fallback_step = s;
-      }
     }
     float ms = 0.f;
     int d = 0;
-    int rc = pmgb_pm_advance(c->pm, 1, &d, &ms);
+    int rc = pmgb_pm_advance(h, 1, &d, &ms);
     total_ms += ms;
-    if (rc == PMGB_EESCAPED) {
-      if (steps_done) *steps_done = done;
-      if (device_ms) *device_ms = total_ms;
-      return rc;
-    }
+    if (rc == PMGB_EESCAPED) return finish(rc);
     if (rc) return rc;
+    if (judge) {
+      float err = 0.f;
+      rc = pmgb_closure_judge(c, judge_stride, &err);  // the learned force this step left
+      if (rc) return rc;
+      if (err > bound) {
+        h->cur = cur0;
+        h->since_sort = since0;
+        h->acc_mode = -1;
+        PMGB_CUDA_TRY(cudaMemcpyAsync(h->pm[cur0], c->save_pm, n * sizeof(float4), cudaMemcpyDeviceToDevice, h->st));
+        PMGB_CUDA_TRY(cudaMemcpyAsync(h->vi[cur0], c->save_vi, n * sizeof(float4), cudaMemcpyDeviceToDevice, h->st));
+        if ((rc = diag_restore(h, c->save_diag))) return rc;
+        set_mode(c, PMGB_CLOSURE_FULL);
+        if (fallback_step) *fallback_step = s;
+        rc = pmgb_pm_advance(h, 1, &d, &ms);
+        total_ms += ms;
+        if (rc == PMGB_EESCAPED) return finish(rc);
+        if (rc) return rc;
+      }
+    }
     ++done;
   }
-  if (steps_done) *steps_done = done;
-  if (device_ms) *device_ms = total_ms;
-  return PMGB_OK;
+  return finish(PMGB_OK);
 }
 
 // test support: features (67 floats per particle, original order) and patch masses

@@ -329,6 +329,23 @@ int diag_after_drift(pmgb_pm* h, int tag) {
 
 int diag_capacity(const pmgb_pm* h) { return h->diag ? h->diag->cap : 0; }
 
+int diag_save(pmgb_pm* h, unsigned char* save) {
+  pmgb_diag* d = h->diag;
+  if (!d) return PMGB_OK;
+  PMGB_CUDA_TRY(cudaMemcpyAsync(save, d->state, 3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  PMGB_CUDA_TRY(cudaMemcpyAsync(save + 3 * sizeof(double), d->count, sizeof(int), cudaMemcpyDeviceToDevice, h->st));
+  return PMGB_OK;
+}
+
+int diag_restore(pmgb_pm* h, const unsigned char* save) {
+  pmgb_diag* d = h->diag;
+  if (!d) return PMGB_OK;
+  PMGB_CUDA_TRY(cudaMemcpyAsync(d->state, save, 3 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  PMGB_CUDA_TRY(cudaMemcpyAsync(d->count, save + 3 * sizeof(double), sizeof(int), cudaMemcpyDeviceToDevice, h->st));
+  d->rho_valid = false;  // the density buffer holds the abandoned step's
+  return PMGB_OK;
+}
+
 void diag_free(pmgb_pm* h) {
   pmgb_diag* d = h->diag;
   if (!d) return;

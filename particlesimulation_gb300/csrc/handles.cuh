@@ -174,6 +174,10 @@ int diag_before_drift(pmgb_pm* h);
 int diag_after_drift(pmgb_pm* h, int tag);
 void diag_free(pmgb_pm* h);
 int diag_capacity(const pmgb_pm* h);
+// The records' running state (expected momentum, record count: 28 bytes into the device buffer
+// `save`) saved before a step and put back to take the step again (the density then recomputed).
+int diag_save(pmgb_pm* h, unsigned char* save);
+int diag_restore(pmgb_pm* h, const unsigned char* save);
 
 // StateRecorder output (recorder.cu): frame of the iteration tagged `tag`, run start / end.
 int rec_begin_run(pmgb_pm* h, int record_field);

@@ -168,18 +168,40 @@ def test_sampled_judge(gpu_lib):
     pm.close()
 
 
-def test_judge_falls_back_to_plain_p3m(gpu_lib):
-    """With a bound no closure can meet, the judged run switches to plain P3M at its first
-    check and then matches a plain-P3M run."""
-    w = _small_disk(n=16384, seed=9)
+def _run_closure(w, mode, steps, bound=1.0, interval=0):
     pm, cl = _closure(w)
     pm.run(0)
-    cl.setMode(cl.LEARNED)
-    esc, done, fallback, _ = cl.run(4, bound=1e-9, judgeInterval=2)
-    assert not esc and done == 4 and fallback == 0
-    assert cl.mode() == cl.FULL
+    cl.setMode(mode)
+    esc, done, fallback, _ = cl.run(steps, bound=bound, judgeInterval=interval)
+    assert not esc and done == steps
+    state = [a.copy() for a in pm.getParticles(units="original")[:2]]
+    final = cl.mode()
     cl.close()
     pm.close()
+    return state, fallback, final
+
+
+def test_judge_falls_back_to_plain_p3m(gpu_lib):
+    """With a bound no closure can meet, the judged run rejects its first step after it ran,
+    takes it again with plain P3M from the step's saved start and stays on plain P3M: its end
+    state equals a plain-P3M run's from the same start bit for bit.  A judge that passes leaves
+    the run as it was: the same as a learned run without judging, bit for bit."""
+    import particlesimulation_gb300 as P
+    w = _small_disk(n=16384, seed=9)
+    full = P.LearnedClosure.FULL
+    learned = P.LearnedClosure.LEARNED
+    fell, fallback, final = _run_closure(w, learned, 4, bound=1e-9, interval=2)
+    assert fallback == 0 and final == full
+    plain, fb, _ = _run_closure(w, full, 4)
+    assert fb == -1
+    for a, b in zip(fell, plain):
+        np.testing.assert_array_equal(a, b)
+    judged, fb, final = _run_closure(w, learned, 4, bound=1.0, interval=2)
+    assert fb == -1 and final == learned
+    unjudged, _, _ = _run_closure(w, learned, 4)
+    for a, b in zip(judged, unjudged):
+        np.testing.assert_array_equal(a, b)
+    assert np.abs(judged[0] - plain[0]).max() > 0  # the learned steps did differ from plain P3M
 
 
 def test_tensor_core_wait_gives_up_and_context_survives(gpu_lib):
