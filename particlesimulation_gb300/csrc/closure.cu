@@ -903,6 +903,9 @@ struct pmgb_closure {
   float* accF = nullptr;        // scratch: 3n floats each
   float* accR = nullptr;
   unsigned char* judged = nullptr;  // n flags: particles a sampled judge pass covered
+  float* jerr = nullptr;        // the judge's relative differences (n), their count
+  unsigned* jcount = nullptr;
+  float* jerr_host = nullptr;   // pinned copy of the differences (n)
   float4* save_pm = nullptr;    // a judged step's start state (n each), to take it again
   float4* save_vi = nullptr;
   unsigned char* save_diag = nullptr;  // and its diagnostics' running state (32 bytes)
@@ -1019,7 +1022,8 @@ int pmgb_closure_create(pmgb_pm* pm, const pmgb_p3m_config* full_cfg, float redu
       (rc = cl_alloc(&c->loss, 1)) || (rc = cl_alloc(&c->img, IMG_SIZE)) ||
       (rc = cl_alloc(&c->X, (size_t)std::max(c->cap, 1) * CL_K0)) ||
       (rc = cl_alloc(&c->T, (size_t)std::max(c->cap, 1) * 4)) || (rc = cl_alloc(&c->accF, 3 * n)) ||
-      (rc = cl_alloc(&c->accR, 3 * n)) || (rc = cl_alloc(&c->judged, n))) {
+      (rc = cl_alloc(&c->accR, 3 * n)) || (rc = cl_alloc(&c->judged, n)) || (rc = cl_alloc(&c->jerr, n)) ||
+      (rc = cl_alloc(&c->jcount, 1))) {
     pmgb_closure_destroy(c);
     return rc;
   }
@@ -1056,9 +1060,10 @@ int pmgb_closure_destroy(pmgb_closure* c) {
   if (c->reduced) pmgb_p3m_destroy(c->reduced);
   void* ptrs[] = {c->occ_fx, c->occ, c->params, c->adam_m, c->adam_v, c->grad, c->gw, c->lossw,
                   c->loss, c->img, c->X, c->T, c->accF, c->accR, c->judged, c->save_pm, c->save_vi,
-                  c->save_diag};
+                  c->save_diag, c->jerr, c->jcount};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  if (c->jerr_host) cudaFreeHost(c->jerr_host);
   delete c;
   return PMGB_OK;
 }
@@ -1176,6 +1181,25 @@ int pmgb_closure_set_params(pmgb_closure* c, const float* params, int count) {
 
 int pmgb_closure_param_count(void) { return CL_NPARAM; }
 
+namespace pmgb {
+// |aR - aF| / |aF| of the judged particles (flags[i] set; without flags every stride-th index),
+// appended in any order to err (count): the components' differences in float, the rest in
+// double without contraction, as the host computed them.
+__global__ void judge_err_kernel(const float* __restrict__ accR, const float* __restrict__ accF,
+                                 const unsigned char* __restrict__ flags, int stride, int n, float* __restrict__ err,
+                                 unsigned* __restrict__ count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !(flags ? flags[i] != 0 : i % stride == 0)) return;
+  const float b0 = accF[3 * i], b1 = accF[3 * i + 1], b2 = accF[3 * i + 2];
+  const double dx = __fsub_rn(accR[3 * i], b0), dy = __fsub_rn(accR[3 * i + 1], b1),
+               dz = __fsub_rn(accR[3 * i + 2], b2);
+  const double nb = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(b0, b0), __dmul_rn(b1, b1)), __dmul_rn(b2, b2)));
+  if (!(nb > 0)) return;
+  const double d = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+  err[atomicAdd(count, 1u)] = (float)__ddiv_rn(d, nb);
+}
+}  // namespace pmgb
+
 // median relative error of the closure force vs the full-cutoff P3M force, over every
 // `stride`-th particle, at the current positions
 int pmgb_closure_judge(pmgb_closure* c, int stride, float* median_rel_err) {
@@ -1203,34 +1227,37 @@ int pmgb_closure_judge(pmgb_closure* c, int stride, float* median_rel_err) {
   rc = force_into(c, PMGB_CLOSURE_FULL, c->accF);
   c->full->unit_stride = 1;
   if (rc) return rc;
-  std::vector<unsigned char> flag(n, 0);
   if (sampled && n) {
     PMGB_CUDA_TRY(cudaMemsetAsync(c->judged, 0, n, h->st));
     rc = launch_mark_sampled(c->full->cell_start, c->full->items, c->full->nitems, c->full->nitems_max, stride,
                              h->vi[h->cur], c->judged, h->st);
     if (rc) return rc;
-    PMGB_CUDA_TRY(cudaMemcpyAsync(flag.data(), c->judged, n, cudaMemcpyDeviceToHost, h->st));
-  } else {
-    for (size_t i = 0; i < n; i += (size_t)stride) flag[i] = 1;
   }
-  std::vector<float> a(3 * n), b(3 * n);
-  PMGB_CUDA_TRY(cudaMemcpyAsync(a.data(), c->accR, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, h->st));
-  PMGB_CUDA_TRY(cudaMemcpyAsync(b.data(), c->accF, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, h->st));
+  // the judged particles' relative differences, on the device; only they come back
+  if (!c->jerr_host && cudaMallocHost(&c->jerr_host, std::max(n, (size_t)1) * sizeof(float)) != cudaSuccess) {
+    c->jerr_host = nullptr;
+    cudaGetLastError();
+    return set_error("cudaMallocHost failed (judge)"), PMGB_ENOMEM;
+  }
+  unsigned count = 0;
+  PMGB_CUDA_TRY(cudaMemsetAsync(c->jcount, 0, sizeof(unsigned), h->st));
+  if (n) {
+    judge_err_kernel<<<(unsigned)((n + 255) / 256), 256, 0, h->st>>>(c->accR, c->accF, sampled ? c->judged : nullptr,
+                                                                     stride, (int)n, c->jerr, c->jcount);
+    PMGB_LAUNCH_CHECK();
+    count_launches(1);
+  }
+  PMGB_CUDA_TRY(cudaMemcpyAsync(&count, c->jcount, sizeof(unsigned), cudaMemcpyDeviceToHost, h->st));
   PMGB_CUDA_TRY(cudaStreamSynchronize(h->st));
-  std::vector<float> e;
-  for (size_t i = 0; i < n; ++i) {
-    if (!flag[i]) continue;
-    const double dx = a[3 * i] - b[3 * i], dy = a[3 * i + 1] - b[3 * i + 1], dz = a[3 * i + 2] - b[3 * i + 2];
-    const double nb = std::sqrt((double)b[3 * i] * b[3 * i] + (double)b[3 * i + 1] * b[3 * i + 1] +
-                                (double)b[3 * i + 2] * b[3 * i + 2]);
-    if (nb > 0) e.push_back((float)(std::sqrt(dx * dx + dy * dy + dz * dz) / nb));
-  }
-  if (e.empty()) {
+  if (count == 0) {
     *median_rel_err = 0.f;
     return PMGB_OK;
   }
-  std::nth_element(e.begin(), e.begin() + e.size() / 2, e.end());
-  *median_rel_err = e[e.size() / 2];
+  PMGB_CUDA_TRY(cudaMemcpyAsync(c->jerr_host, c->jerr, count * sizeof(float), cudaMemcpyDeviceToHost, h->st));
+  PMGB_CUDA_TRY(cudaStreamSynchronize(h->st));
+  // the median of the multiset: the same whatever order the kernel appended them in
+  std::nth_element(c->jerr_host, c->jerr_host + count / 2, c->jerr_host + count);
+  *median_rel_err = c->jerr_host[count / 2];
   return PMGB_OK;
 }
 

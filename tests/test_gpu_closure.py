@@ -164,6 +164,11 @@ def test_sampled_judge(gpu_lib):
     d = np.linalg.norm(acc[cl.LEARNED] - acc[cl.FULL], axis=1) / np.linalg.norm(acc[cl.FULL], axis=1)
     full_median = float(np.median(d))
     assert 0.7 * full_median < j_fresh < 1.4 * full_median, (j_fresh, full_median)
+    # every particle (stride 1: an unsampled pass), the learned force of the last evaluation:
+    # the device-side differences give numpy's median over all particles (the upper middle
+    # element against the mean of the two middle ones)
+    j_all = cl.judge(stride=1)
+    assert abs(j_all - full_median) <= 1e-3 * full_median, (j_all, full_median)
     cl.close()
     pm.close()
 
