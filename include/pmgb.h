@@ -307,7 +307,7 @@ int pmgb_p3m_set_symmetric(pmgb_p3m* p3m, int enable);
 int pmgb_p3m_get_symmetric(pmgb_p3m* p3m, int* enabled, unsigned int* units_last_pass);
 /* Sub-columns per cell axis the pair pass splits each chaining-mesh cell into (x and z): 1 for
  * the reference's unsorted lists; with y-sorted lists 5 where the handle's particles average at
- * least 48 per cell (N >= 48 Mx My Mz), 4 from 32, else 3, lowered (not below 3) until the
+ * least 96 per cell (N >= 96 Mx My Mz), 4 from 32, else 3, lowered (not below 3) until the
  * symmetric slots fit a quarter of the free device memory.  Fixed at creation.  The cell lists
  * handed out (pmgb_p3m_get_cell_lists) are whole cells either way.  No reference counterpart. */
 int pmgb_p3m_get_subcolumns(const pmgb_p3m* p3m, int* per_axis);

@@ -640,16 +640,16 @@ int p3m_create_internal(pmgb_pm* pm, const pmgb_p3m_config* cfg, pmgb_p3m** out,
   q->ncells = q->cd.Mx * q->cd.My * q->cd.Mz;
   // Sub-columns per cell axis when the lists are y-sorted (the pair pass prunes by x-z gap and y
   // window per sub-column, and its symmetric part pairs sub-columns): 5 where the particles
-  // average at least 48 per cell, 4 from 32, else 3.  Pair pass on the disk workloads, 3 / 4 / 5
-  // sub-columns, by mean particles per cell: 14: 28.0 / 28.4 / 30.3 ms; 28: 6.00 / 6.10 / 6.65;
-  // 39: 47.7 / 44.7 / 45.4; 60: 60.1 / 56.7 / 55.8; 113: 89.4 / 80.2 / 76.5 (2 x 2 was slower
+  // average at least 96 per cell, 4 from 32, else 3.  Pair pass on the disk workloads, 3 / 4 / 5
+  // sub-columns, by mean particles per cell: 14: 26.3 / 27.0 / 29.1 ms; 28: 5.59 / 5.63 / 6.07;
+  // 39: 43.8 / 42.4 / 43.5; 60: 56.9 / 52.9 / 53.6; 113: 87.6 / 74.2 / 73.8 (2 x 2 was slower
   // throughout).  A finer split only where its symmetric slots (27 sub^2 x 16 B per particle)
   // stay within a quarter of the free device memory (the rule the allocation below applies).
   // The reference's unsorted fill order keeps whole cells.
   q->cd.sub = 1;
   if (cfg->y_sorting) {
     const long long n = pm->n, nc = q->ncells;
-    q->cd.sub = n >= 48 * nc ? 5 : n >= 32 * nc ? 4 : 3;
+    q->cd.sub = n >= 96 * nc ? 5 : n >= 32 * nc ? 4 : 3;
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
       free_b = 0;

@@ -203,7 +203,7 @@ def _sym_case(n, table, seed, grid=64, spread=(0.6, 2.5)):
 
 
 @pytest.mark.parametrize("table,n,grid,sub", [(1, 20000, 64, 3), (0, 20000, 64, 3), (1, 40000, 64, 4),
-                                              (0, 40000, 64, 4), (1, 60000, 64, 5), (0, 60000, 32, 5)])
+                                              (0, 60000, 64, 4), (1, 60000, 32, 5), (0, 60000, 32, 5)])
 def test_symmetric_pass_matches_one_sided(gpu_lib, table, n, grid, sub):
     """The pair pass's symmetric part (light sub-column pairs evaluated once, each side into a
     slot of its own, summed in a fixed order): it takes a large share of the pairs here, its
@@ -246,7 +246,7 @@ def test_symmetric_pass_matches_one_sided(gpu_lib, table, n, grid, sub):
 @pytest.mark.parametrize("grid,n,ysort,sub", [(64, 20000, 1, 3), (64, 40000, 1, 4), (32, 30000, 1, 5),
                                               (32, 30000, 0, 1)])
 def test_subcolumns_per_cell_and_cell_lists(gpu_lib, grid, n, ysort, sub):
-    """Sub-columns per cell axis: 5 where the particles average at least 48 per chaining-mesh cell,
+    """Sub-columns per cell axis: 5 where the particles average at least 96 per chaining-mesh cell,
     4 from 32, else 3, 1 for the reference's unsorted lists; the cell lists handed out are the
     reference's whole-cell lists either way (vs the oracle's ChainingMesh fill, bit for bit)."""
     cfg, q, pos, vel, mass = _sym_case(n, 1, seed=31, grid=grid)
@@ -262,7 +262,7 @@ def test_subcolumns_per_cell_and_cell_lists(gpu_lib, grid, n, ysort, sub):
     assert dims == d_ref
     if ysort:
         nc = int(np.prod(dims))
-        assert sub == (5 if n >= 48 * nc else 4 if n >= 32 * nc else 3)
+        assert sub == (5 if n >= 96 * nc else 4 if n >= 32 * nc else 3)
     np.testing.assert_array_equal(counts, c_ref)
     np.testing.assert_array_equal(order, o_ref)
     p3m.close()
