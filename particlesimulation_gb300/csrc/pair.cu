@@ -601,7 +601,10 @@ __device__ __forceinline__ bool sym_dead(const u32* __restrict__ masks, int word
   return (__ldg(&masks[(size_t)a * words + words - 1]) >> k) & 1u;
 }
 
-// Marks and units, one thread per sub-column a (a = nsub: the bucket outside the mesh, no marks).
+// Marks and units, one warp at a time per sub-column a (a = nsub: the bucket outside the mesh, no
+// marks; the warps stride over the sub-columns, most of which are empty or sparse); lane l of
+// round t looks at mark bit 32 t + l (direction k, neighbour sub-column cb), so a round's ballot
+// is one mask word.
 // Each unit is staged as (p, q, bucket, position in its bucket); sym_scatter_kernel then lays
 // the buckets out one after the other in units.  If more than cap units are listed, the pass
 // runs one-sided.
@@ -615,58 +618,58 @@ __global__ void sym_plan_kernel(const int* __restrict__ cs, ChainDimsP cd, int n
                                 u32* __restrict__ masks, uint4* __restrict__ stage, u32 cap,
                                 u32* __restrict__ counter, const int* __restrict__ stop) {
   constexpr int MW = sym_mark_words(L) + 1;
+  static_assert(MW <= 32, "one mask word per lane");
   if (*stop) return;
-  const int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a > nsub) return;
-  u32 w[MW];
-#pragma unroll
-  for (int i = 0; i < MW; ++i) w[i] = 0u;
-  const int pa = a < nsub ? cs[a + 1] - cs[a] : 0;
-  if (pa >= SYM_MIN_SMALL) {
-    const unsigned long long thr = __ldcg(reinterpret_cast<const unsigned long long*>(counter + 6));
-    const int cell = a / L, ca = a % L;
-    const int gx = cell % cd.Mx, gy = (cell / cd.Mx) % cd.My, gz = cell / (cd.Mx * cd.My);
-    u32 dead = 0u;
-    for (int k = 0; k < NNB; ++k) {
-      const int nx = gx + k % 3 - 1, ny = gy + (k / 3) % 3 - 1, nz = gz + k / 9 - 1;
-      if (nx < 0 || ny < 0 || nz < 0 || nx >= cd.Mx || ny >= cd.My || nz >= cd.Mz) {
-        dead |= 1u << k;
-        continue;
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+  for (int a = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); a <= nsub; a += nwarps) {
+    const int pa = a < nsub ? __ldg(&cs[a + 1]) - __ldg(&cs[a]) : 0;
+    u32 word = 0u;  // lane t < MW - 1: mark word t; lane MW - 1: the dead directions
+    if (pa >= SYM_MIN_SMALL) {
+      const unsigned long long thr = __ldcg(reinterpret_cast<const unsigned long long*>(counter + 6));
+      const int cell = a / L, ca = a % L;
+      const int gx = cell % cd.Mx, gy = (cell / cd.Mx) % cd.My, gz = cell / (cd.Mx * cd.My);
+      u32 alive = 0u;  // bit k: something one-sided left toward neighbour cell k (this lane's bits)
+#pragma unroll 1
+      for (int t = 0; t < MW - 1; ++t) {
+        const int sb = 32 * t + lane;
+        bool marked = false;
+        if (sb < NNB * L) {
+          const int k = sb / L, cb = sb % L;
+          const int nx = gx + k % 3 - 1, ny = gy + (k / 3) % 3 - 1, nz = gz + k / 9 - 1;
+          if (nx >= 0 && ny >= 0 && nz >= 0 && nx < cd.Mx && ny < cd.My && nz < cd.Mz) {
+            const int b = (nx + ny * cd.Mx + nz * cd.Mx * cd.My) * L + cb;
+            const int pb = b == a ? 0 : __ldg(&cs[b + 1]) - __ldg(&cs[b]);
+            if (b == a) {
+              alive |= 1u << k;
+            } else if (pb > 0 && sym_gap2(cd, gx, gz, ca, nx, nz, cb, margin) < re2) {
+              const unsigned long long cost = (unsigned long long)pa * (unsigned long long)pb;
+              if (pb < SYM_MIN_SMALL || max(pa, pb) < SYM_MIN_BIG || cost >= thr * SYM_CTA_MUL) {
+                alive |= 1u << k;
+              } else {
+                marked = true;
+                if (k > 13 || (k == 13 && cb > ca)) {
+                  const int bk = sym_bucket(cost, thr);
+                  const u32 pos = atomicAdd(&counter[SLOT_SYM_COUNT + bk], 1u);
+                  const u32 idx = atomicAdd(&counter[SLOT_SYM_TOTAL], 1u);
+                  if (idx < cap)
+                    stage[idx] = pa >= pb ? make_uint4((u32)a, (u32)b, (u32)bk, pos)
+                                          : make_uint4((u32)b, (u32)a, (u32)bk, pos);
+                }
+              }
+            }
+          }
+        }
+        const u32 bits = __ballot_sync(0xFFFFFFFFu, marked);
+        if (lane == t) word = bits;
       }
-      const int nb = nx + ny * cd.Mx + nz * cd.Mx * cd.My;
-      bool alive = false;  // something one-sided left toward this neighbour cell
-#pragma unroll
-      for (int cb = 0; cb < L; ++cb) {
-        const int b = nb * L + cb;
-        if (b == a) {
-          alive = true;
-          continue;
-        }
-        const int pb = __ldg(&cs[b + 1]) - __ldg(&cs[b]);
-        if (pb == 0 || sym_gap2(cd, gx, gz, ca, nx, nz, cb, margin) >= re2) continue;
-        const unsigned long long cost = (unsigned long long)pa * (unsigned long long)pb;
-        if (pb < SYM_MIN_SMALL || max(pa, pb) < SYM_MIN_BIG || cost >= thr * SYM_CTA_MUL) {
-          alive = true;
-          continue;
-        }
-        const int sb = k * L + cb;
-#pragma unroll
-        for (int i = 0; i < MW - 1; ++i)
-          if ((sb >> 5) == i) w[i] |= 1u << (sb & 31);
-        if (k > 13 || (k == 13 && cb > ca)) {
-          const int bk = sym_bucket(cost, thr);
-          const u32 pos = atomicAdd(&counter[SLOT_SYM_COUNT + bk], 1u);
-          const u32 idx = atomicAdd(&counter[SLOT_SYM_TOTAL], 1u);
-          if (idx < cap)
-            stage[idx] = pa >= pb ? make_uint4((u32)a, (u32)b, (u32)bk, pos) : make_uint4((u32)b, (u32)a, (u32)bk, pos);
-        }
-      }
-      if (!alive) dead |= 1u << k;
+      // a direction with nothing one-sided left (out of the mesh, or every sub-column empty, out
+      // of reach or marked) is dead
+      const u32 alive_all = __reduce_or_sync(0xFFFFFFFFu, alive);
+      if (lane == MW - 1) word = ~alive_all & ((1u << NNB) - 1u);
     }
-    w[MW - 1] = dead;
+    if (lane < MW) masks[(size_t)a * MW + lane] = word;
   }
-#pragma unroll
-  for (int i = 0; i < MW; ++i) masks[(size_t)a * MW + i] = w[i];
 }
 
 // subcol[i] = the sub-column (or the outside bucket) of sorted particle i.
@@ -1301,8 +1304,8 @@ int launch_pair(const float4* pm, const float4* vi, const float4* acc_pm, const 
       // units buffer: 2 cap uint2 of staging (as cap uint4), then the laid-out list
       uint4* stage = reinterpret_cast<uint4*>(sym->units);
       auto plan = chd.sub == 5 ? sym_plan_kernel<25> : chd.sub == 4 ? sym_plan_kernel<16> : sym_plan_kernel<9>;
-      plan<<<(nsub + 1 + 255) / 256, 256, 0, st>>>(cell_start, cd, nsub, pp.re2, 1e-3f * fminf(cd.HCsx, cd.HCsz),
-                                                  sym->masks, stage, sym->cap, counter, stop);
+      plan<<<std::min((nsub + 1 + 7) / 8, num_sms * 16), 256, 0, st>>>(
+          cell_start, cd, nsub, pp.re2, 1e-3f * fminf(cd.HCsx, cd.HCsz), sym->masks, stage, sym->cap, counter, stop);
       sym_scatter_kernel<<<num_sms * 4, 256, 0, st>>>(stage, sym->units + 2 * (size_t)sym->cap, sym->cap, counter,
                                                        stop);
       subcol_kernel<<<pb, 256, 0, st>>>(cell_start, items, nitems, sym->subcol, stop);
