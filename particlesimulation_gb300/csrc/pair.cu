@@ -825,16 +825,41 @@ __device__ __forceinline__ void sym_unit(const SlotCtx& c, float4* __restrict__ 
   float4* __restrict__ sj = sym_slots + (size_t)((NNB - 1 - k) * L + ca) * c.n;
   const float h0 = sqrtf(c.re2 - sym_gap2(cd, gx, gz, ca, nx, nz, cb, c.gap_margin));
   const int bb = c.cell_start[q], be = c.cell_start[q + 1];
+  const int p0 = c.cell_start[p], cend = c.cell_start[p + 1];
+  // the y window in q of the slice starting at i0: the cutoff chord at the sub-columns' gap
+  // around the slice's y range, widened by 1e-5 of the coordinates' size against float rounding
+  auto window = [&](int i0, int& jb, int& je) {
+    const float ys0 = __ldg(&c.pm[i0].y), ys1 = __ldg(&c.pm[min(i0 + SYM_SLICE - 1, cend - 1)].y);
+    const float h = h0 + 1e-5f * (1.f + fabsf(ys1));
+    jb = bb;
+    je = be;
+    if (c.ysort && je > jb) {
+      jb = warp_y_bound<false>(c.pm, jb, je, ys0 - h, lane);
+      je = warp_y_bound<true>(c.pm, jb, je, ys1 + h, lane);
+    }
+  };
+  // COOP: one warp finds each slice's window for the whole CTA (the first before the unit's
+  // barrier, the next while four other warps add up the current slice's i sides) instead of
+  // every warp searching the same one
+  __shared__ int s_win[2];
+  constexpr int WIN_WARP = SLOT_WARPS - 1;
   if (COOP) {
     for (int j = bb + (int)threadIdx.x; j < be; j += SLOT_THREADS) sj[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (warp == WIN_WARP) {
+      int jb, je;
+      window(p0, jb, je);
+      if (lane == 0) {
+        s_win[0] = jb;
+        s_win[1] = je;
+      }
+    }
     __syncthreads();
   } else {
     for (int j = bb + lane; j < be; j += 32) sj[j] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncwarp();
   }
-  const int cend = c.cell_start[p + 1];
   const float sc = c.sc;
-  for (int i0 = c.cell_start[p]; i0 < cend; i0 += SYM_SLICE) {
+  for (int i0 = p0; i0 < cend; i0 += SYM_SLICE) {
     const int last = min(i0 + SYM_SLICE - 1, cend - 1);
     SymI I[SYM_IPL];
     float w[SYM_IPL];
@@ -857,11 +882,12 @@ __device__ __forceinline__ void sym_unit(const SlotCtx& c, float4* __restrict__ 
       I[u].y = (I[u].y - ys0) * sc;
       I[u].z = (I[u].z - oz) * sc;
     }
-    const float h = h0 + 1e-5f * (1.f + fabsf(ys1));
-    int jb = bb, je = be;
-    if (c.ysort && je > jb) {
-      jb = warp_y_bound<false>(c.pm, jb, je, ys0 - h, lane);
-      je = warp_y_bound<true>(c.pm, jb, je, ys1 + h, lane);
+    int jb, je;
+    if (COOP) {
+      jb = s_win[0];
+      je = s_win[1];
+    } else {
+      window(i0, jb, je);
     }
     if (i0 + SYM_SLICE <= cend)
       sym_window<EXACT, false, COOP>(c, I, w, jb, je, ox, ys0, oz, sj, jbuf, tab_base, lane, warp);
@@ -878,6 +904,14 @@ __device__ __forceinline__ void sym_unit(const SlotCtx& c, float4* __restrict__ 
       for (int u = 0; u < SYM_IPL; ++u)
         part[warp * SYM_SLICE + 32 * u + lane] = make_float4(I[u].sx, I[u].sy, I[u].sz, 0.f);
       __syncthreads();
+      if (warp == WIN_WARP && i0 + SYM_SLICE < cend) {  // the next slice's window
+        int jb2, je2;
+        window(i0 + SYM_SLICE, jb2, je2);
+        if (lane == 0) {
+          s_win[0] = jb2;
+          s_win[1] = je2;
+        }
+      }
       if (threadIdx.x < SYM_SLICE) {
         float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
 #pragma unroll 4
