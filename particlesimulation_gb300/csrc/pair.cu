@@ -433,28 +433,54 @@ __device__ __forceinline__ void slot_unit(const SlotCtx& c, u32 it, float4 (*jbu
       I[u].p.z = (I[u].p.z - oz) * sc;
     }
     int chunk = 0;  // COOP: candidate chunks met so far in this unit
-    if (nx >= 0 && ny >= 0 && nz >= 0 && nx < cd.Mx && ny < cd.My && nz < cd.Mz)
-    for (int qs = 0; qs < sub2; ++qs) {
+    const bool nin = nx >= 0 && ny >= 0 && nz >= 0 && nx < cd.Mx && ny < cd.My && nz < cd.Mz;
+    // the candidates [b, e) of neighbour sub-column qs (false: out of reach or taken by the
+    // symmetric units); a warp-collective search
+    auto qwin = [&](int qs, int& b, int& e) -> bool {
       const int jsx = qs % sub, jsz = qs / sub;
       const float jx0 = (nx * sub + jsx) * cd.HCsx, jz0 = (nz * sub + jsz) * cd.HCsz;
       const float gxs = fmaxf(fmaxf(jx0 - (ix0 + cd.HCsx), ix0 - (jx0 + cd.HCsx)) - c.gap_margin, 0.f);
       const float gzs = fmaxf(fmaxf(jz0 - (iz0 + cd.HCsz), iz0 - (jz0 + cd.HCsz)) - c.gap_margin, 0.f);
       const float g2 = gxs * gxs + gzs * gzs;
-      if (g2 >= c.re2) continue;
+      if (g2 >= c.re2) return false;
       if (c.sym_masks) {
         const int sb = k * sub2 + qs;
-        if ((__ldg(&c.sym_masks[(size_t)item.x * c.sym_words + (sb >> 5)]) >> (sb & 31)) & 1u) continue;
+        if ((__ldg(&c.sym_masks[(size_t)item.x * c.sym_words + (sb >> 5)]) >> (sb & 31)) & 1u) return false;
       }
       // a pair in range has |dy|^2 < re^2 - (its x-z distance)^2 <= re^2 - g2: the y window
       // of this sub-column is the chord of the cutoff sphere at the sub-column's x-z gap, widened
       // by 1e-5 of the coordinates' size against float rounding of the comparisons
       const float h = sqrtf(c.re2 - g2) + 1e-5f * (1.f + fabsf(ys1));
       const int cn = (nx + ny * cd.Mx + nz * cd.Mx * cd.My) * sub2 + qs;
-      int b = c.cell_start[cn];
-      int e = c.cell_start[cn + 1];
+      b = c.cell_start[cn];
+      e = c.cell_start[cn + 1];
       if (c.ysort && e > b) {
         b = warp_y_bound<false>(c.pm, b, e, ys0 - h, lane);
         e = warp_y_bound<true>(c.pm, b, e, ys1 + h, lane);
+      }
+      return true;
+    };
+    // COOP: the warps find the sub-columns' windows once for the CTA (warp w those of sub-columns
+    // w, w + SLOT_WARPS), instead of every warp searching all of them
+    __shared__ int2 s_qwin[32];
+    if (COOP && nin) {
+      for (int qs = warp; qs < sub2; qs += SLOT_WARPS) {
+        int b = 0, e = 0;
+        if (!qwin(qs, b, e)) b = e = 0;
+        if (lane == 0) s_qwin[qs] = make_int2(b, e);
+      }
+      __syncthreads();
+    }
+    if (nin)
+    for (int qs = 0; qs < sub2; ++qs) {
+      int b, e;
+      if (COOP) {
+        const int2 w = s_qwin[qs];
+        b = w.x;
+        e = w.y;
+        if (e <= b) continue;
+      } else if (!qwin(qs, b, e)) {
+        continue;
       }
       // COOP: this warp's chunks of the window are c = first, first + SLOT_WARPS, ... where
       // chunk + first = warp (mod SLOT_WARPS)
